@@ -1,0 +1,120 @@
+/*
+ * gsks.h -- GB300 extensions of the GSKS C ABI (libgsks.so).
+ *
+ * ks.h keeps the reference's interface unchanged.  This header adds what the
+ * reference has no counterpart for, or reports through printf/exit:
+ *   - status codes and gsks_last_error() (the reference prints and exits,
+ *     frame/dgsks.c:465-467, frame/omp_dgsks_list.cpp:321-324,
+ *     frame/ks_util.c:50-51);
+ *   - a precision switch: plain FP64 or split-precision tensor-core form;
+ *   - device-resident entry points taking device pointers and a CUDA stream;
+ *   - dgsks_list, a flat C-ABI batched call over CSR task lists (the
+ *     reference only has the C++ std::vector interface of
+ *     include/omp_dgsks_list.hpp:48-115, which forwards here).
+ *
+ * All entry points are plain C: pointers, sizes and a stream handle passed as
+ * void*.  They are thread-safe; every calling host thread gets its own CUDA
+ * stream, staging buffers and workspace on the current device.
+ */
+#ifndef GSKS_GB300_GSKS_H
+#define GSKS_GB300_GSKS_H
+
+#include <stddef.h>
+#include "ks.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ------------------------------------------------------------ */
+enum {
+  GSKS_OK = 0,
+  GSKS_ERR_ARG = 1,          /* negative size, NULL array that is needed      */
+  GSKS_ERR_KERNEL_TYPE = 2,  /* ks_t.type outside ks_type                     */
+  GSKS_ERR_BANDWIDTH = 3,    /* var-bandwidth Gaussian without hi/hj          */
+  GSKS_ERR_LAPLACE_K = 4,    /* Laplace needs k > 2                           */
+  GSKS_ERR_MAP_RANGE = 5,    /* a map index is negative or beyond the pool    */
+  GSKS_ERR_CUDA = 6,         /* a CUDA runtime call failed                    */
+  GSKS_ERR_ALLOC = 7,        /* host or device allocation failed              */
+  GSKS_ERR_LIST = 8,         /* inconsistent task lists                       */
+  GSKS_ERR_PRECISION = 9,    /* unknown precision, or form not built          */
+  GSKS_ERR_NO_DEVICE = 10,   /* no CUDA device visible                        */
+  GSKS_ERR_TOO_LARGE = 11    /* a size beyond what the entry point supports   */
+};
+
+/* Status of the calling thread's most recent GSKS call. */
+int gsks_last_error(void);
+/* Static description of a status code. */
+const char *gsks_error_string(int code);
+
+/* ---- precision --------------------------------------------------------- */
+enum {
+  GSKS_FP64 = 0,        /* FP64 rank-k, FP64 kernel function and sums        */
+  GSKS_SPLIT_BF16X3 = 1 /* split 3xBF16 tensor-core rank-k, FP32 kernel
+                           function, FP64 norms / near-pair distances / u    */
+};
+
+/* Precision used by dgsks()/dgsks_list() on the calling thread.  The
+ * initial value comes from GSKS_PRECISION ("fp64" or "split"). */
+int gsks_set_precision(int precision);
+int gsks_get_precision(void);
+
+/* dgsks() with a status return (same arguments as ks.h dgsks). */
+int dgsks_status(ks_t *kernel, int m, int n, int k,
+                 double *u, int *umap,
+                 double *XA, double *XA2, int *amap,
+                 double *XB, double *XB2, int *bmap,
+                 double *w, int *wmap);
+
+/* ---- device-resident entry points ------------------------------------- */
+/* All arrays are device pointers on the current device; `stream` is a
+ * cudaStream_t (NULL = the legacy default stream).  kernel->hi / hj must be
+ * device pointers too.  The call is asynchronous with respect to the host:
+ * it enqueues its kernels on `stream` and returns.  umap must not repeat an
+ * index within one call (each target row owns its u entry).  XA2/XB2 may be
+ * NULL for the inner-product kernels (polynomial, tanh).  Workspace is held
+ * by the calling thread's context and reused across calls.
+ * nxa / nxb: pool sizes used to range-check the maps on the device (pass -1
+ * to skip the check). */
+int gsks_dgsks_device(ks_t *kernel, int m, int n, int k,
+                      double *u, const int *umap,
+                      const double *XA, const double *XA2, const int *amap, int nxa,
+                      const double *XB, const double *XB2, const int *bmap, int nxb,
+                      const double *w, const int *wmap,
+                      int precision, void *stream);
+
+/* Squared norms X2[p] = sum_q X[p*k+q]^2 of N device-resident points. */
+int gsks_norms_device(int N, int k, const double *X, double *X2, void *stream);
+
+/* Number of kernels the last device call of this thread enqueued. */
+int gsks_last_launch_count(void);
+
+/* Waits for the device, then returns and clears the device-side error flags
+ * of the calling thread's context (bit 0: a map index outside [0, nxa/nxb)
+ * was clamped and skipped by gsks_dgsks_device).  Returns -1 if the flags
+ * could not be read. */
+int gsks_device_errors(void);
+
+/* ---- batched evaluation ------------------------------------------------ */
+/* dgsks_list: ntask independent kernel summations accumulated into one u.
+ * Task t evaluates, for a in [a_off[t], a_off[t+1]) and b in [b_off[t], b_off[t+1]),
+ *     u[u_idx[a]] += K(XA[a_idx[a]], XB[b_idx[b]]) * w[w_idx[b]]
+ * Contributions of different tasks to the same u entry are summed in a fixed
+ * order (deterministic).  kernels: NULL to use `kernel` for every task, or an
+ * array of ntask descriptors (per-task kernel type and parameters).  u_idx
+ * may be NULL (= a_idx) and w_idx may be NULL (= b_idx).  XA2/XB2 may be NULL,
+ * in which case the norms are computed on the device.  Host or device arrays
+ * (all of one kind).  nu/nxa/nxb/nw: sizes of u, the two pools and w. */
+int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
+               double *u, int nu,
+               const int *a_off, const int *a_idx, const int *u_idx,
+               const int *b_off, const int *b_idx, const int *w_idx,
+               double *XA, double *XA2, int nxa,
+               double *XB, double *XB2, int nxb,
+               double *w, int nw);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSKS_GB300_GSKS_H */

@@ -1,0 +1,485 @@
+// gsks_api.cu -- the C ABI of libgsks.so (ks.h + gsks.h).
+//
+// Host-side layer between C callers and the sm_103a kernels:
+//   * argument and kernel-descriptor checks with status codes in place of
+//     the reference's printf + exit (frame/dgsks.c:393-468);
+//   * per-thread contexts (CUDA stream, pinned staging, device buffers), so
+//     that dgsks() may be called concurrently from many host threads as the
+//     reference's batched driver does (frame/omp_dgsks_list.cpp:366-396);
+//   * host-pointer calls: the rows named by the maps are gathered into pinned
+//     buffers, copied once, evaluated with identity maps, and u is scattered
+//     back in target order (u[umap[i]] = result[i], i ascending,
+//     frame/dgsks_ref.c:454-459).  umap is meant to be injective within one
+//     call; for repeated entries this path keeps the last writer, whereas the
+//     reference's result then depends on its OpenMP schedule and blocking;
+//   * device-pointer calls run in place on the caller's stream.
+#include "gsks.h"
+#include "gsks_internal.cuh"
+#include "gsks_host.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace gsks {
+
+thread_local int tl_status = GSKS_OK;
+thread_local int tl_precision = -1;
+thread_local int tl_launches = 0;
+
+static bool verbose()
+{
+  static int v = -1;
+  if (v < 0) { const char *e = getenv("GSKS_VERBOSE"); v = (e && *e && *e != '0') ? 1 : 0; }
+  return v == 1;
+}
+
+int set_status(int s, const char *where)
+{
+  tl_status = s;
+  if (s != GSKS_OK && verbose())
+    fprintf(stderr, "gsks: %s: %s\n", where ? where : "", gsks_error_string(s));
+  return s;
+}
+
+int cuda_status(cudaError_t e, const char *where)
+{
+  if (e == cudaSuccess) return GSKS_OK;
+  if (verbose()) fprintf(stderr, "gsks: %s: %s\n", where, cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return set_status(GSKS_ERR_ALLOC, where);
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    return set_status(GSKS_ERR_NO_DEVICE, where);
+  return set_status(GSKS_ERR_CUDA, where);
+}
+
+void note_launches(int n) { tl_launches = n; }
+
+// ---------------------------------------------------------------------------
+bool DevBuf::ensure(size_t bytes)
+{
+  if (bytes <= cap) return true;
+  if (p) { cudaFree(p); p = nullptr; cap = 0; }
+  size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+  if (cudaMalloc(&p, want) != cudaSuccess) { p = nullptr; return false; }
+  cap = want;
+  return true;
+}
+void DevBuf::release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+
+bool PinBuf::ensure(size_t bytes)
+{
+  if (bytes <= cap) return true;
+  if (p) { cudaFreeHost(p); p = nullptr; cap = 0; }
+  size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+  if (cudaMallocHost(&p, want) != cudaSuccess) { p = nullptr; return false; }
+  cap = want;
+  return true;
+}
+void PinBuf::release() { if (p) cudaFreeHost(p); p = nullptr; cap = 0; }
+
+Ctx::~Ctx()
+{
+  // Runs at host-thread exit; the CUDA runtime may already be gone at
+  // process teardown, in which case the frees fail harmlessly.
+  for (DevBuf *b : {&partial, &err, &dA, &dA2, &dB, &dB2, &dw, &du, &dhi, &dhj, &dwork})
+    b->release();
+  for (PinBuf *b : {&hA, &hA2, &hB, &hB2, &hw, &hu, &hhi, &hhj}) b->release();
+  if (stream) cudaStreamDestroy(stream);
+}
+
+static thread_local std::unique_ptr<Ctx> tl_ctx;
+
+Ctx *get_ctx()
+{
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) { cuda_status(e, "cudaGetDevice"); return nullptr; }
+  if (tl_ctx && tl_ctx->device == dev) return tl_ctx.get();
+  std::unique_ptr<Ctx> c(new Ctx);
+  c->device = dev;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    cuda_status(e, "cudaStreamCreate");
+    return nullptr;
+  }
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (!c->err.ensure(sizeof(int))) { set_status(GSKS_ERR_ALLOC, "context"); return nullptr; }
+  cudaMemset(c->err.p, 0, sizeof(int));
+  tl_ctx = std::move(c);
+  return tl_ctx.get();
+}
+
+int effective_precision()
+{
+  if (tl_precision < 0) {
+    const char *e = getenv("GSKS_PRECISION");
+    tl_precision = GSKS_FP64;
+    if (e && (!strncmp(e, "split", 5) || !strcmp(e, "bf16x3"))) tl_precision = GSKS_SPLIT_BF16X3;
+  }
+  return tl_precision;
+}
+
+// Kernel-descriptor checks and the Laplace parameter overwrite
+// (frame/dgsks.c:420-468; the reference prints and carries on for a missing
+// bandwidth vector or k < 3, and exits for an illegal type).
+int check_kernel(ks_t *ker, int k)
+{
+  if (!ker) return GSKS_ERR_ARG;
+  switch (ker->type) {
+    case KS_GAUSSIAN: case KS_POLYNOMIAL: case KS_TANH: case KS_QUARTIC:
+    case KS_MULTIQUADRATIC: case KS_EPANECHNIKOV:
+      return GSKS_OK;
+    case KS_GAUSSIAN_VAR_BANDWIDTH:
+      return (ker->hi && ker->hj) ? GSKS_OK : GSKS_ERR_BANDWIDTH;
+    case KS_LAPLACE:
+      if (k < 3) return GSKS_ERR_LAPLACE_K;
+      ker->powe = 0.5 * (2.0 - (double)k);
+      ker->scal = tgamma(0.5 * k + 1.0) / ((double)k * (double)(k - 2) * pow(M_PI, 0.5 * k));
+      return GSKS_OK;
+    default:
+      return GSKS_ERR_KERNEL_TYPE;
+  }
+}
+
+bool is_device_pointer(const void *p)
+{
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return false; }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+static int host_threads_for(size_t work)
+{
+#ifdef _OPENMP
+  if (work < (1u << 16)) return 1;
+  return std::max(1, std::min(omp_get_max_threads(), 16));
+#else
+  (void)work;
+  return 1;
+#endif
+}
+
+// Gather the rows a host-pointer call names into pinned buffers and copy
+// them to the device.  On return `v` describes packed, identity-mapped data.
+int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
+               const double *u, const int *umap,
+               const double *XA, const double *XA2, const int *amap,
+               const double *XB, const double *XB2, const int *bmap,
+               const double *w, const int *wmap, Staged &v)
+{
+  const bool norms = kt_uses_norms(ker->type);
+  const bool varbw = ker->type == KS_GAUSSIAN_VAR_BANDWIDTH;
+  for (int i = 0; i < m; i++)
+    if (amap[i] < 0 || umap[i] < 0) return GSKS_ERR_MAP_RANGE;
+  for (int j = 0; j < n; j++)
+    if (bmap[j] < 0 || wmap[j] < 0) return GSKS_ERR_MAP_RANGE;
+  if (norms && (!XA2 || !XB2)) return GSKS_ERR_ARG;
+
+  const size_t mk = (size_t)m * k, nk = (size_t)n * k;
+  bool ok = c->hA.ensure(mk * 8) && c->hB.ensure(nk * 8) && c->hu.ensure((size_t)m * 8) &&
+            c->hw.ensure((size_t)n * 8) && c->dA.ensure(mk * 8) && c->dB.ensure(nk * 8) &&
+            c->du.ensure((size_t)m * 8) && c->dw.ensure((size_t)n * 8);
+  if (ok && norms)
+    ok = c->hA2.ensure((size_t)m * 8) && c->hB2.ensure((size_t)n * 8) &&
+         c->dA2.ensure((size_t)m * 8) && c->dB2.ensure((size_t)n * 8);
+  if (ok && varbw)
+    ok = c->hhi.ensure((size_t)m * 8) && c->hhj.ensure((size_t)n * 8) &&
+         c->dhi.ensure((size_t)m * 8) && c->dhj.ensure((size_t)n * 8);
+  if (!ok) return GSKS_ERR_ALLOC;
+
+  double *hA = (double *)c->hA.p, *hB = (double *)c->hB.p;
+  double *hA2 = (double *)c->hA2.p, *hB2 = (double *)c->hB2.p;
+  double *hhi = (double *)c->hhi.p, *hhj = (double *)c->hhj.p;
+  double *hu = (double *)c->hu.p, *hw = (double *)c->hw.p;
+  const size_t rowb = (size_t)k * sizeof(double);
+
+  int nt = host_threads_for(mk);
+#pragma omp parallel for num_threads(nt) schedule(static)
+  for (int i = 0; i < m; i++) {
+    const int p = amap[i];
+    memcpy(hA + (size_t)i * k, XA + (size_t)p * k, rowb);
+    if (norms) hA2[i] = XA2[p];
+    if (varbw) hhi[i] = ker->hi[p];
+    hu[i] = u[umap[i]];
+  }
+  nt = host_threads_for(nk);
+#pragma omp parallel for num_threads(nt) schedule(static)
+  for (int j = 0; j < n; j++) {
+    const int p = bmap[j];
+    memcpy(hB + (size_t)j * k, XB + (size_t)p * k, rowb);
+    if (norms) hB2[j] = XB2[p];
+    if (varbw) hhj[j] = ker->hj[p];
+    hw[j] = w[wmap[j]];
+  }
+
+  cudaStream_t s = c->stream;
+  cudaError_t e = cudaSuccess;
+#define GSKS_CP(dst, src, bytes) \
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s)
+  GSKS_CP(c->dA.p, hA, mk * 8);
+  GSKS_CP(c->dB.p, hB, nk * 8);
+  GSKS_CP(c->du.p, hu, (size_t)m * 8);
+  GSKS_CP(c->dw.p, hw, (size_t)n * 8);
+  if (norms) { GSKS_CP(c->dA2.p, hA2, (size_t)m * 8); GSKS_CP(c->dB2.p, hB2, (size_t)n * 8); }
+  if (varbw) { GSKS_CP(c->dhi.p, hhi, (size_t)m * 8); GSKS_CP(c->dhj.p, hhj, (size_t)n * 8); }
+#undef GSKS_CP
+  if (e != cudaSuccess) return cuda_status(e, "stage_host copy");
+
+  v.A = (const double *)c->dA.p; v.B = (const double *)c->dB.p;
+  v.A2 = norms ? (const double *)c->dA2.p : nullptr;
+  v.B2 = norms ? (const double *)c->dB2.p : nullptr;
+  v.hi = varbw ? (const double *)c->dhi.p : nullptr;
+  v.hj = varbw ? (const double *)c->dhj.p : nullptr;
+  v.u = (double *)c->du.p; v.w = (const double *)c->dw.p;
+  return GSKS_OK;
+}
+
+// Copy the evaluated u back and scatter it in target order.
+int unstage_host(Ctx *c, int m, double *u, const int *umap)
+{
+  cudaError_t e = cudaMemcpyAsync(c->hu.p, c->du.p, (size_t)m * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_status(e, "unstage_host");
+  const double *hu = (const double *)c->hu.p;
+  for (int i = 0; i < m; i++) u[umap[i]] = hu[i];
+  return GSKS_OK;
+}
+
+int read_device_errors(Ctx *c)
+{
+  int flags = 0;
+  if (cudaMemcpyAsync(&flags, c->err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess)
+    return -1;
+  cudaStreamSynchronize(c->stream);
+  if (flags) cudaMemsetAsync(c->err.p, 0, sizeof(int), c->stream);
+  return flags;
+}
+
+KParams make_kparams(const ks_t *ker, const double *hi, const double *hj)
+{
+  KParams kp;
+  kp.type = ker->type; kp.scal = ker->scal; kp.cons = ker->cons; kp.powe = ker->powe;
+  kp.hi = hi; kp.hj = hj;
+  kp.coinc = 0.0;
+  return kp;
+}
+
+// Relative size of the rounding noise of the assembled squared distance:
+// |fl(aa - 2 x.y + bb) - d2| <= ~2k u (aa + bb) with u = 2^-53.
+double coincidence_eps(int k) { return 4.0 * (double)std::max(k, 1) * 0x1p-53; }
+
+// Enqueue one fused evaluation on stream s.  Maps may be nullptr (identity).
+int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
+                  double *u, const int *umap,
+                  const double *XA, const double *XA2, const int *amap, int nxa,
+                  const double *XB, const double *XB2, const int *bmap, int nxb,
+                  const double *w, const int *wmap, const double *hi, const double *hj,
+                  int precision, cudaStream_t s, bool stream_ordered_alloc)
+{
+  if (precision == GSKS_SPLIT_BF16X3)
+    return enqueue_split(c, ker, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb,
+                         w, wmap, hi, hj, s, stream_ordered_alloc);
+  if (precision != GSKS_FP64) return GSKS_ERR_PRECISION;
+
+  Fp64Plan p = fp64_plan(m, n, k, c->num_sms);
+  double *partial = nullptr;
+  if (stream_ordered_alloc) {
+    cudaError_t e = cudaMallocAsync((void **)&partial, p.partial_elems * sizeof(double), s);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMallocAsync");
+  } else {
+    if (!c->partial.ensure(p.partial_elems * sizeof(double))) return GSKS_ERR_ALLOC;
+    partial = (double *)c->partial.p;
+  }
+  FusedArgs a{};
+  a.m = m; a.n = n; a.k = k;
+  a.XA = XA; a.XA2 = XA2; a.amap = amap;
+  a.XB = XB; a.XB2 = XB2; a.bmap = bmap;
+  a.w = w; a.wmap = wmap;
+  a.kp = make_kparams(ker, hi, hj);
+  a.kp.coinc = coincidence_eps(k);
+  a.nxa = nxa; a.nxb = nxb;
+  a.partial = partial;
+  a.err = (int *)c->err.p;
+  int launches = fp64_launch(a, p, u, umap, s);
+  if (launches < 0) return GSKS_ERR_KERNEL_TYPE;
+  cudaError_t e = cudaGetLastError();
+  if (stream_ordered_alloc) cudaFreeAsync(partial, s);
+  if (e != cudaSuccess) return cuda_status(e, "fp64 launch");
+  note_launches(launches);
+  return GSKS_OK;
+}
+
+}  // namespace gsks
+
+using namespace gsks;
+
+// ===========================================================================
+extern "C" {
+
+int gsks_last_error(void) { return tl_status; }
+
+const char *gsks_error_string(int code)
+{
+  switch (code) {
+    case GSKS_OK: return "success";
+    case GSKS_ERR_ARG: return "invalid argument";
+    case GSKS_ERR_KERNEL_TYPE: return "illegal kernel type";
+    case GSKS_ERR_BANDWIDTH: return "bandwidth vector has not been initialized";
+    case GSKS_ERR_LAPLACE_K: return "laplace kernel only supports k > 2";
+    case GSKS_ERR_MAP_RANGE: return "map index out of range";
+    case GSKS_ERR_CUDA: return "CUDA runtime error";
+    case GSKS_ERR_ALLOC: return "allocation failed";
+    case GSKS_ERR_LIST: return "alist, blist and wlist must have the same sizes";
+    case GSKS_ERR_PRECISION: return "unsupported precision";
+    case GSKS_ERR_NO_DEVICE: return "no CUDA device";
+    case GSKS_ERR_TOO_LARGE: return "size exceeds the supported maximum";
+    default: return "unknown status";
+  }
+}
+
+int gsks_set_precision(int precision)
+{
+  if (precision != GSKS_FP64 && precision != GSKS_SPLIT_BF16X3)
+    return set_status(GSKS_ERR_PRECISION, "gsks_set_precision");
+  tl_precision = precision;
+  return set_status(GSKS_OK, nullptr);
+}
+
+int gsks_get_precision(void) { return effective_precision(); }
+
+int gsks_last_launch_count(void) { return tl_launches; }
+
+int gsks_device_errors(void)
+{
+  Ctx *c = get_ctx();
+  if (!c) return -1;
+  if (cudaDeviceSynchronize() != cudaSuccess) return -1;
+  return read_device_errors(c);
+}
+
+int dgsks_status(ks_t *kernel, int m, int n, int k,
+                 double *u, int *umap,
+                 double *XA, double *XA2, int *amap,
+                 double *XB, double *XB2, int *bmap,
+                 double *w, int *wmap)
+{
+  tl_launches = 0;
+  if (m < 0 || n < 0 || k < 0) return set_status(GSKS_ERR_ARG, "dgsks");
+  // early return before the kernel-type switch, as frame/dgsks.c:394-397
+  if (m == 0 || n == 0 || k == 0) return set_status(GSKS_OK, nullptr);
+  int st = check_kernel(kernel, k);
+  if (st) return set_status(st, "dgsks");
+  if (!u || !umap || !XA || !amap || !XB || !bmap || !w || !wmap)
+    return set_status(GSKS_ERR_ARG, "dgsks");
+  Ctx *c = get_ctx();
+  if (!c) return tl_status;
+  const int prec = effective_precision();
+
+  if (is_device_pointer(XA)) {
+    st = enqueue_fused(c, kernel, m, n, k, u, umap, XA, XA2, amap, -1, XB, XB2, bmap, -1,
+                       w, wmap, kernel->hi, kernel->hj, prec, c->stream, false);
+    if (st) return set_status(st, "dgsks");
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(e, "dgsks");
+    return set_status(GSKS_OK, nullptr);
+  }
+
+  Staged v;
+  st = stage_host(c, kernel, m, n, k, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap, v);
+  if (st) return set_status(st, "dgsks");
+  st = enqueue_fused(c, kernel, m, n, k, v.u, nullptr, v.A, v.A2, nullptr, m, v.B, v.B2,
+                     nullptr, n, v.w, nullptr, v.hi, v.hj, prec, c->stream, false);
+  if (st) return set_status(st, "dgsks");
+  st = unstage_host(c, m, u, umap);
+  return set_status(st, "dgsks");
+}
+
+void dgsks(ks_t *kernel, int m, int n, int k,
+           double *u, int *umap,
+           double *XA, double *XA2, int *amap,
+           double *XB, double *XB2, int *bmap,
+           double *w, int *wmap)
+{
+  (void)dgsks_status(kernel, m, n, k, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap);
+}
+
+int gsks_dgsks_device(ks_t *kernel, int m, int n, int k,
+                      double *u, const int *umap,
+                      const double *XA, const double *XA2, const int *amap, int nxa,
+                      const double *XB, const double *XB2, const int *bmap, int nxb,
+                      const double *w, const int *wmap,
+                      int precision, void *stream)
+{
+  tl_launches = 0;
+  if (m < 0 || n < 0 || k < 0) return set_status(GSKS_ERR_ARG, "gsks_dgsks_device");
+  if (m == 0 || n == 0 || k == 0) return set_status(GSKS_OK, nullptr);
+  int st = check_kernel(kernel, k);
+  if (st) return set_status(st, "gsks_dgsks_device");
+  if (!u || !XA || !XB || !w) return set_status(GSKS_ERR_ARG, "gsks_dgsks_device");
+  if (kt_uses_norms(kernel->type) && (!XA2 || !XB2))
+    return set_status(GSKS_ERR_ARG, "gsks_dgsks_device");
+  Ctx *c = get_ctx();
+  if (!c) return tl_status;
+  st = enqueue_fused(c, kernel, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb,
+                     w, wmap, kernel->hi, kernel->hj, precision, (cudaStream_t)stream, true);
+  return set_status(st, "gsks_dgsks_device");
+}
+
+int gsks_norms_device(int N, int k, const double *X, double *X2, void *stream)
+{
+  if (N < 0 || k < 0 || (N > 0 && (!X || !X2))) return set_status(GSKS_ERR_ARG, "gsks_norms_device");
+  cudaError_t e = norms_launch(N, k, X, X2, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "gsks_norms_device");
+  tl_launches = N > 0 ? 1 : 0;
+  return set_status(GSKS_OK, nullptr);
+}
+
+double *ks_malloc_aligned(int m, int n, int size)
+{
+  void *ptr = nullptr;
+  size_t bytes = (size_t)(m > 0 ? m : 0) * (size_t)(n > 0 ? n : 0) * (size_t)(size > 0 ? size : 0);
+  if (bytes == 0) bytes = 64;
+  if (posix_memalign(&ptr, 64, bytes) != 0) {
+    set_status(GSKS_ERR_ALLOC, "ks_malloc_aligned");
+    return nullptr;
+  }
+  set_status(GSKS_OK, nullptr);
+  return (double *)ptr;
+}
+
+static ks_t wrapper_kernel(int type, double scal, double cons, double powe, double *h)
+{
+  ks_t ker;
+  memset(&ker, 0, sizeof(ker));
+  ker.type = (ks_type)type;
+  ker.scal = scal; ker.cons = cons; ker.powe = powe;
+  ker.hi = h; ker.hj = h; ker.h = h;
+  return ker;
+}
+
+void dgsks_wrapper(int m, int n, int k, double *u, int *umap,
+                   double *XA, double *XA2, int *amap,
+                   double *XB, double *XB2, int *bmap,
+                   double *w, int *wmap,
+                   int type, double scal, double cons, double powe, double *h)
+{
+  ks_t ker = wrapper_kernel(type, scal, cons, powe, h);
+  dgsks(&ker, m, n, k, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap);
+}
+
+void dgsks_ref_wrapper(int m, int n, int k, double *u, int *umap,
+                       double *XA, double *XA2, int *amap,
+                       double *XB, double *XB2, int *bmap,
+                       double *w, int *wmap,
+                       int type, double scal, double cons, double powe, double *h)
+{
+  ks_t ker = wrapper_kernel(type, scal, cons, powe, h);
+  dgsks_ref(&ker, m, n, k, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap);
+}
+
+}  // extern "C"

@@ -1,0 +1,76 @@
+// gsks_host.h -- host-side context and helpers shared by the C-ABI units.
+#pragma once
+
+#include <cstddef>
+#include <cuda_runtime.h>
+#include "ks.h"
+#include "gsks_internal.cuh"
+
+namespace gsks {
+
+// Growable device / pinned host buffers owned by a per-thread context.
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  bool ensure(size_t bytes);
+  void release();
+};
+struct PinBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  bool ensure(size_t bytes);
+  void release();
+};
+
+// Per host thread, per device: stream, error flags, staging and workspace.
+struct Ctx {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  DevBuf partial, err;
+  DevBuf dA, dA2, dB, dB2, dw, du, dhi, dhj, dwork;
+  PinBuf hA, hA2, hB, hB2, hw, hu, hhi, hhj;
+  ~Ctx();
+};
+
+// Packed, identity-mapped device copy of a host-pointer call.
+struct Staged {
+  const double *A = nullptr, *A2 = nullptr, *B = nullptr, *B2 = nullptr;
+  const double *hi = nullptr, *hj = nullptr, *w = nullptr;
+  double *u = nullptr;
+};
+
+Ctx *get_ctx();
+int set_status(int s, const char *where);
+int cuda_status(cudaError_t e, const char *where);
+void note_launches(int n);
+int effective_precision();
+int check_kernel(ks_t *ker, int k);
+bool is_device_pointer(const void *p);
+KParams make_kparams(const ks_t *ker, const double *hi, const double *hj);
+double coincidence_eps(int k);
+int read_device_errors(Ctx *c);
+
+int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
+               const double *u, const int *umap,
+               const double *XA, const double *XA2, const int *amap,
+               const double *XB, const double *XB2, const int *bmap,
+               const double *w, const int *wmap, Staged &v);
+int unstage_host(Ctx *c, int m, double *u, const int *umap);
+
+int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
+                  double *u, const int *umap,
+                  const double *XA, const double *XA2, const int *amap, int nxa,
+                  const double *XB, const double *XB2, const int *bmap, int nxb,
+                  const double *w, const int *wmap, const double *hi, const double *hj,
+                  int precision, cudaStream_t s, bool stream_ordered_alloc);
+
+// Split-precision form (gsks_split.cu).
+int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k,
+                  double *u, const int *umap,
+                  const double *XA, const double *XA2, const int *amap, int nxa,
+                  const double *XB, const double *XB2, const int *bmap, int nxb,
+                  const double *w, const int *wmap, const double *hi, const double *hj,
+                  cudaStream_t s, bool stream_ordered_alloc);
+
+}  // namespace gsks
