@@ -95,6 +95,13 @@ int gsks_last_launch_count(void);
  * could not be read. */
 int gsks_device_errors(void);
 
+/* ---- calibration -------------------------------------------------------- */
+/* Measured issue rate of one pipe of the current device, in operations per
+ * second (an FMA counts as one operation): what = 0 FP64 FMA, 1 FP32 FMA,
+ * 2 SFU ex2.  Used for the roofline fractions the benchmark reports; the
+ * reference has no counterpart. */
+int gsks_probe_peak(int what, double *ops_per_s);
+
 /* ---- batched evaluation ------------------------------------------------ */
 /* dgsks_list: ntask independent kernel summations accumulated into one u.
  * Task t evaluates, for a in [a_off[t], a_off[t+1]) and b in [b_off[t], b_off[t+1]),

@@ -28,7 +28,39 @@ struct KParams {
   // the |x|^2 - 2 x.y + |y|^2 form, i.e. the points coincide; it takes the
   // reference's coincident-point clamp (frame/dgsks_ref.c:343-345).
   double coinc;
+  // Exponent class of powe (polynomial, Laplace): integer and half-integer
+  // exponents up to 64 in magnitude are evaluated by binary powering (and one
+  // square root) instead of the general pow().
+  int pmode, pint;
 };
+
+enum { POW_GENERAL = 0, POW_INT = 1, POW_HALF = 2 };
+
+// x^e for 0 <= e <= 64 by binary powering: at most 2 log2(e) multiplies, a
+// relative error of a few units in the last place.
+__device__ __forceinline__ double pow_upos(double x, int e)
+{
+  double r = 1.0;
+  for (;;) {
+    if (e & 1) r *= x;
+    e >>= 1;
+    if (!e) break;
+    x *= x;
+  }
+  return r;
+}
+
+// x^powe with the exponent class chosen on the host.
+__device__ __forceinline__ double pow_class(double x, const KParams &kp)
+{
+  if (kp.pmode == POW_INT)
+    return kp.pint >= 0 ? pow_upos(x, kp.pint) : 1.0 / pow_upos(x, -kp.pint);
+  if (kp.pmode == POW_HALF) {
+    const double r = sqrt(x);
+    return kp.pint >= 0 ? pow_upos(x, kp.pint) * r : r / pow_upos(x, -kp.pint);
+  }
+  return pow(x, kp.powe);
+}
 
 // Everything one fused evaluation needs.  Maps may be nullptr, which means
 // the identity (position i of the call is pool point i).
@@ -68,11 +100,11 @@ __device__ __forceinline__ double kfun64(double dot, double aa, double bb,
     double c = fma(dot, kp.scal, kp.cons);
     if (kp.powe == 2.0) return c * c;
     if (kp.powe == 4.0) { c = c * c; return c * c; }
-    return pow(c, kp.powe);
+    return pow_class(c, kp);
   } else if constexpr (KT == KS_LAPLACE) {
     double d2 = fma(-2.0, dot, aa) + bb;
     if (d2 < fmax(1e-15, kp.coinc * (aa + bb))) d2 = 1.79e308;
-    return pow(d2, kp.powe) * kp.scal;
+    return pow_class(d2, kp) * kp.scal;
   } else if constexpr (KT == KS_TANH) {
     return tanh(fma(dot, kp.scal, kp.cons));
   } else if constexpr (KT == KS_QUARTIC) {

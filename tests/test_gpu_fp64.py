@@ -99,6 +99,9 @@ def test_general_stride_config2_shape(gpu, oracle_mod, ktype, params):
     from ks_gb300 import gsks
     O = oracle_mod
     X, X2, w, amap, bmap, umap, wmap = _random_case(7, 12000, 64, 3000, 2500)
+    # norms summed in the same order as the oracle's inner products, so that
+    # coincident points cancel exactly there (Laplace is singular at d2 = 0)
+    X2 = O.norms(X)
     u_ref = np.zeros(12000)
     O.dgsks(O.make_kernel(ktype, **params), u_ref, umap, X, X2, amap, X, X2, bmap, w, wmap)
     _, cond = O.rows(O.make_kernel(ktype, **params), np.arange(3000, dtype=np.int32), X, X2, amap, X, X2, bmap, w, wmap)

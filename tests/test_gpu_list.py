@@ -53,9 +53,10 @@ def test_list_per_task_kernels_and_separate_maps(gpu, oracle_mod):
     O = oracle_mod
     rng = np.random.default_rng(5)
     N, k, ntask = 3000, 16, 40
-    X = rng.random((N, k)); X2 = (X * X).sum(1); w = rng.standard_normal(N)
+    X = rng.random((N, k)); X2 = O.norms(X); w = rng.standard_normal(N)
     a_off, a_idx, b_off, b_idx = _lists(rng, N, ntask, 0, 400)
-    u_idx = rng.integers(0, N, a_idx.size).astype(np.int32)
+    # u entries are distinct within a task and shared across tasks
+    u_idx = np.concatenate([rng.permutation(N)[:a_off[t + 1] - a_off[t]] for t in range(ntask)]).astype(np.int32)
     w_idx = rng.integers(0, N, b_idx.size).astype(np.int32)
     specs = []
     for t in range(ntask):
