@@ -83,6 +83,24 @@ int gsks_dgsks_device(ks_t *kernel, int m, int n, int k,
                       const double *w, const int *wmap,
                       int precision, void *stream);
 
+/* gsks_dgsks_device() for callers that cannot let a library allocate device
+ * memory -- e.g. a process whose device memory is reserved up front by its
+ * own pool allocator, or a loop that may not allocate after start-up.  No
+ * counterpart in the reference (its dgsks allocates host pack buffers on
+ * every call).  FP64 form only, arguments as gsks_dgsks_device without the
+ * precision and pool sizes (maps are not range-checked).  Its scratch is a
+ * fixed 8 MiB array inside the library, so m may be at most 1048576
+ * (GSKS_ERR_TOO_LARGE otherwise).  The first call on a device looks up that
+ * array's device address; make it before any stream capture.  All calls on a
+ * device share the array: calls that overlap on the GPU race, so serialise
+ * them.  Allocates nothing: no cudaMalloc, cudaFree or allocating library
+ * call, and no stream or context of its own; enqueues on `stream`. */
+int gsks_dgsks_device_noalloc(ks_t *kernel, int m, int n, int k,
+                              double *u, const int *umap,
+                              const double *XA, const double *XA2, const int *amap,
+                              const double *XB, const double *XB2, const int *bmap,
+                              const double *w, const int *wmap, void *stream);
+
 /* Squared norms X2[p] = sum_q X[p*k+q]^2 of N device-resident points. */
 int gsks_norms_device(int N, int k, const double *X, double *X2, void *stream);
 
