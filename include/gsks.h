@@ -120,6 +120,19 @@ int gsks_device_errors(void);
  * reference has no counterpart. */
 int gsks_probe_peak(int what, double *ops_per_s);
 
+/* ---- diagnostics -------------------------------------------------------- */
+/* Test hook of the split-precision form (no counterpart in the reference):
+ * runs one device-resident evaluation like gsks_dgsks_device with
+ * GSKS_SPLIT_BF16X3 and writes, for the first tile of the first CTA, the raw
+ * tensor-core accumulators and the epilogue values of every (row, column) to
+ * `dump` (128*128*5 floats: H, L, K, t, lo) and the call's scales to
+ * `params_out` (alpha, sigma, 1/sigma, q as doubles at byte 0, the centre
+ * (k doubles) at byte 64).  Device pointers. */
+int gsks_split_debug_dump(ks_t *kernel, int m, int n, int k, double *u, const int *umap,
+                          const double *XA, const int *amap, const double *XB, const int *bmap,
+                          const double *w, const int *wmap, float *dump, void *params_out,
+                          void *stream);
+
 /* ---- batched evaluation ------------------------------------------------ */
 /* dgsks_list: ntask independent kernel summations accumulated into one u.
  * Task t evaluates, for a in [a_off[t], a_off[t+1]) and b in [b_off[t], b_off[t+1]),

@@ -1,0 +1,83 @@
+"""Split-precision tensor-core form (tcgen05) against the FP64 oracle.
+
+Tolerance 1e-6 on the normwise and the conditioned max-relative error
+max_i |du_i| / sum_j |K_ij w_j| (the gate of the split form)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+SPLIT = 1
+
+
+def _case(seed, N, k, m, n, dist="unif"):
+    rng = np.random.default_rng(seed)
+    if dist == "unif":
+        X = rng.random((N, k))
+    else:
+        X = rng.standard_normal((N, k))
+    w = rng.standard_normal(N)
+    amap = rng.choice(N, m, replace=False).astype(np.int32)
+    bmap = rng.choice(N, n, replace=False).astype(np.int32)
+    umap = rng.permutation(N)[:m].astype(np.int32)
+    wmap = rng.permutation(N)[:n].astype(np.int32)
+    return X, w, amap, bmap, umap, wmap
+
+
+def _run(gpu, O, ktype, params, X, w, amap, bmap, umap, wmap, hi=None):
+    from ks_gb300 import gsks
+    torch = gpu
+    N, k = X.shape
+    m, n = amap.size, bmap.size
+    X2 = O.norms(X)
+    okern = dict(params)
+    if hi is not None:
+        okern.update(hi=hi, hj=hi)
+    u_ref = np.zeros(N)
+    O.dgsks(O.make_kernel(ktype, **okern), u_ref, umap, X, X2, amap, X, X2, bmap, w, wmap)
+    _, cond = O.rows(O.make_kernel(ktype, **okern), np.arange(m, dtype=np.int32), X, X2, amap, X, X2, bmap, w, wmap)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    gk = dict(params)
+    if hi is not None:
+        hd = t(hi)
+        gk.update(hi=hd, hj=hd)
+    u = torch.zeros(N, dtype=torch.float64, device="cuda")
+    gsks.dgsks_device(gsks.make_kernel(ktype, **gk), m, n, k, u, t(umap), t(X), t(X2), t(amap), t(X), t(X2),
+                      t(bmap), t(w), t(wmap), precision=SPLIT, stream=torch.cuda.current_stream(), nxa=N, nxb=N)
+    torch.cuda.synchronize()
+    assert gsks.device_errors() == 0
+    got = u.cpu().numpy()
+    return O.errors(got[umap], u_ref[umap], cond=cond)
+
+
+@pytest.mark.parametrize("shape", [(500, 16, 128, 128), (700, 16, 128, 256), (3000, 8, 300, 1000),
+                                   (5000, 64, 1000, 1500), (4000, 3, 513, 700), (4000, 37, 200, 333)])
+def test_split_gaussian_uniform(gpu, oracle_mod, shape):
+    N, k, m, n = shape
+    e = _run(gpu, oracle_mod, 0, dict(scal=-2.0), *_case(1, N, k, m, n))
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+@pytest.mark.parametrize("ktype,params", [
+    (1, dict(scal=1 / 16, cons=1.0, powe=3.0)), (1, dict(scal=0.1, cons=0.1, powe=4.0)),
+    (2, {}), (4, dict(scal=0.1, cons=0.1)), (6, dict(cons=1.0)),
+])
+def test_split_other_kernels(gpu, oracle_mod, ktype, params):
+    e = _run(gpu, oracle_mod, ktype, params, *_case(2, 3000, 16, 700, 900))
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+@pytest.mark.parametrize("ktype", [5, 7])
+def test_split_compact_kernels(gpu, oracle_mod, ktype):
+    X, w, amap, bmap, umap, wmap = _case(3, 3000, 16, 700, 900)
+    e = _run(gpu, oracle_mod, ktype, {}, X * 0.2, w, amap, bmap, umap, wmap)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+def test_split_var_bandwidth(gpu, oracle_mod):
+    X, w, amap, bmap, umap, wmap = _case(4, 4000, 8, 900, 1100)
+    rng = np.random.default_rng(44)
+    h = np.exp(rng.uniform(np.log(0.05), np.log(0.5), X.shape[0]))
+    e = _run(gpu, oracle_mod, 3, {}, X, w, amap, bmap, umap, wmap, hi=1.0 / h)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
