@@ -1,31 +1,33 @@
 #!/usr/bin/env python
-"""Kernel pair-evaluations per second of GSKS on GB300.
+"""Kernel pair-evaluations per second of GSKS on GB300: split-precision
+tensor-core form against the plain FP64 form, with errors and rooflines.
 
 Workload (the general-stride configuration of the benchmark spec): a pool of
 N = 262144 points in k = 64 dimensions drawn uniform[0,1] (FP64), m = n =
 65536 targets / sources chosen as random subsets of the pool (amap, bmap),
 u / w maps random permutations of [0, 65536), weights N(0,1).  One step
-evaluates the three kernels of that configuration on it, each a full
-m x n summation into u:
-    Gaussian h = 0.5 (scal = -1/(2h^2) = -2), Laplace (powe, scal from k),
-    polynomial (scal = 1/k, cons = 1, powe = 3).
-Synthetic, seeded inputs of the specified shapes and distributions.
+evaluates the three kernels of that configuration, each a full m x n
+summation into u: Gaussian h = 0.5 (scal = -1/(2h^2) = -2), Laplace (powe,
+scal from k), polynomial (scal = 1/k, cons = 1, powe = 3).  Synthetic, seeded
+inputs of the specified shapes and distributions.
 
-Reported:
-  value     pair-evals/s over the timed steps, inputs resident in HBM, through
-            gsks_dgsks_device (CUDA events on the launch stream, L2 flushed
-            between steps by a 512 MiB memset);
-  e2e       the same through ks.h dgsks() with host arrays: gather, host->device
-            copies, kernels and the device->host copy of u inside the region;
-  roofline  per kernel type against the measured pipe rate that binds it;
-  cpu_baseline  the CPU port of the reference's fused dgsks (oracle) on all
-            host cores, on sampled target rows x all sources; its row sums
-            also give the error of the GPU result on those rows.
+Reported (one JSON line):
+  value      pair-evals/s of the split-precision form, inputs resident in HBM,
+             through gsks_dgsks_device (CUDA events on the launch stream, L2
+             flushed between steps by a 512 MiB memset inside the region);
+  forms      the same for the split and the plain FP64 form, their ratio and
+             their per-kernel times;
+  e2e        the split form through ks.h dgsks() with host arrays (gather,
+             host->device copies, kernels, device->host copy of u);
+  roofline   per form and kernel against the measured pipe that binds it;
+  cpu_baseline  the oracle's port of the reference's fused dgsks on all host
+             cores over sampled target rows x all sources; its row sums also
+             give the errors of both forms (normwise and conditioned).
   --impl reference times that CPU implementation alone (the reference's own
-  code does not build on the aarch64 host: its micro-kernels are AVX).
+  micro-kernels are AVX and do not build on the aarch64 host).
 
-Multi-GPU (torchrun): every rank runs an independent replica of the workload
-(no data-path collective); value = all pairs / max-over-ranks time.
+Multi-GPU (torchrun): every rank runs an independent replica (no data-path
+collective); value = all ranks' pairs / max-over-ranks time.
 """
 from __future__ import annotations
 
@@ -36,7 +38,6 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -52,6 +53,7 @@ KERNELS = [
 ]
 WORKLOAD = ("general stride: pool 262144 x k=64 uniform[0,1] FP64; m=n=65536 random subsets; "
             "u/w maps random permutations of [0,65536); Gaussian h=0.5 + Laplace + polynomial pwr=3")
+SPLIT_PRODUCTS = 6   # tensor-core products per slice pair set (a1b1, a1b2, a2b1, a2b2, a1b3, a3b1)
 
 
 def parse():
@@ -60,50 +62,36 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--forms", default="split,fp64", help="forms to time; the first is the headline")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--case", default=None, choices=[k[0] for k in KERNELS],
                     help="profiling case: only device calls of one kernel type (for ncu)")
+    ap.add_argument("--precision", default="split", choices=["fp64", "split"], help="form of --case")
     ap.add_argument("--m", type=int, default=M_T)
     ap.add_argument("--n", type=int, default=N_S)
     ap.add_argument("--reps", type=int, default=2)
     return ap.parse_args()
 
 
-def run_case(args):
-    """A small device-resident case of one kernel type, for ncu captures: the
-    configuration's pool and k, m x n targets/sources, `reps` calls."""
-    import torch
-    from ks_gb300 import build as B
-    if not os.path.exists(B.LIB):
-        B.build()
-    from ks_gb300 import gsks
-    torch.cuda.set_device(0)
-    wl = make_workload(torch)
-    prec = gsks.GSKS_FP64 if args.precision == "fp64" else gsks.GSKS_SPLIT_BF16X3
-    name, kt, p, _f = [k for k in KERNELS if k[0] == args.case][0]
-    u = torch.zeros(M_T, dtype=torch.float64, device="cuda")
-    for _ in range(args.reps):
-        gsks.dgsks_device(gsks.make_kernel(kt, **p), args.m, args.n, K_DIM, u, wl["umap"], wl["X"], wl["X2"],
-                          wl["amap"], wl["X"], wl["X2"], wl["bmap"], wl["w"], wl["wmap"], precision=prec,
-                          stream=torch.cuda.current_stream(), nxa=N_POOL, nxb=N_POOL)
-    torch.cuda.synchronize()
-    print(json.dumps({"case": name, "m": args.m, "n": args.n, "reps": args.reps, "precision": args.precision,
-                      "u_norm": float(u.norm())}))
+def peaks_file():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 # ---------------------------------------------------------------------------
-def dist_setup(args):
+def dist_setup():
     import torch
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
-        backend = "nccl" if torch.cuda.is_available() else "gloo"
-        dist.init_process_group(backend=backend)
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
     if torch.cuda.is_available():
         torch.cuda.set_device(local)
     return ws, rank, local
@@ -125,7 +113,6 @@ def max_over_ranks(ws, x: float) -> float:
     return float(t.item())
 
 
-# ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -133,8 +120,7 @@ class ClockSampler:
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
-        self.index = index
-        self.proc = None
+        self.index, self.proc, self.lines = index, None, []
 
     def __enter__(self):
         try:
@@ -146,7 +132,6 @@ class ClockSampler:
         return self
 
     def __exit__(self, *exc):
-        self.lines = []
         if self.proc:
             self.proc.terminate()
             try:
@@ -154,12 +139,12 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
                 out, _ = self.proc.communicate()
-            self.lines = [l for l in out.splitlines() if l.strip()]
+            self.lines += [l for l in out.splitlines() if l.strip()]
 
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in getattr(self, "lines", []):
+        for l in self.lines:
             f = [x.strip() for x in l.split(",")]
             if len(f) < 9:
                 continue
@@ -172,131 +157,122 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
 # ---------------------------------------------------------------------------
 def make_workload(torch, seed=1234):
+    from ks_gb300 import gsks
     g = torch.Generator(device="cuda")
     g.manual_seed(seed)
-    dev = "cuda"
-    X = torch.rand(N_POOL, K_DIM, dtype=torch.float64, device=dev, generator=g)
-    X2 = torch.empty(N_POOL, dtype=torch.float64, device=dev)
-    from ks_gb300 import gsks
+    X = torch.rand(N_POOL, K_DIM, dtype=torch.float64, device="cuda", generator=g)
+    X2 = torch.empty(N_POOL, dtype=torch.float64, device="cuda")
     gsks.norms_device(X, X2, stream=torch.cuda.current_stream())
-    amap = torch.randperm(N_POOL, device=dev, generator=g)[:M_T].to(torch.int32)
-    bmap = torch.randperm(N_POOL, device=dev, generator=g)[:N_S].to(torch.int32)
-    umap = torch.randperm(M_T, device=dev, generator=g).to(torch.int32)
-    wmap = torch.randperm(N_S, device=dev, generator=g).to(torch.int32)
-    w = torch.randn(N_S, dtype=torch.float64, device=dev, generator=g)
+    amap = torch.randperm(N_POOL, device="cuda", generator=g)[:M_T].to(torch.int32)
+    bmap = torch.randperm(N_POOL, device="cuda", generator=g)[:N_S].to(torch.int32)
+    umap = torch.randperm(M_T, device="cuda", generator=g).to(torch.int32)
+    wmap = torch.randperm(N_S, device="cuda", generator=g).to(torch.int32)
+    w = torch.randn(N_S, dtype=torch.float64, device="cuda", generator=g)
     torch.cuda.synchronize()
     return dict(X=X, X2=X2, amap=amap, bmap=bmap, umap=umap, wmap=wmap, w=w)
 
 
-def kernel_desc(gsks, ktype, params):
-    return gsks.make_kernel(ktype, **params)
+def prec_of(gsks, form):
+    return gsks.GSKS_FP64 if form == "fp64" else gsks.GSKS_SPLIT_BF16X3
 
 
-def run_ours(args, ws, rank, local):
-    import numpy as np
+def device_call(gsks, wl, kt, p, u, prec, stream, m=M_T, n=N_S):
+    gsks.dgsks_device(gsks.make_kernel(kt, **p), m, n, K_DIM, u, wl["umap"], wl["X"], wl["X2"], wl["amap"],
+                      wl["X"], wl["X2"], wl["bmap"], wl["w"], wl["wmap"], precision=prec, stream=stream,
+                      nxa=N_POOL, nxb=N_POOL)
+    return gsks.last_launch_count()
+
+
+def run_case(args):
+    """A device-resident case of one kernel type, for ncu captures."""
     import torch
     from ks_gb300 import build as B
     if not os.path.exists(B.LIB):
         B.build()
     from ks_gb300 import gsks
-    lib = gsks.load()
-    prec = gsks.GSKS_FP64 if args.precision == "fp64" else gsks.GSKS_SPLIT_BF16X3
+    torch.cuda.set_device(0)
     wl = make_workload(torch)
-    stream = torch.cuda.current_stream()
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    name, kt, p, _f = [k for k in KERNELS if k[0] == args.case][0]
+    u = torch.zeros(M_T, dtype=torch.float64, device="cuda")
+    for _ in range(args.reps):
+        device_call(gsks, wl, kt, p, u, prec_of(gsks, args.precision), torch.cuda.current_stream(), args.m, args.n)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": name, "m": args.m, "n": args.n, "reps": args.reps, "precision": args.precision,
+                      "u_norm": float(u.norm())}))
 
-    # measured pipe rates for the roofline
-    dfma = C.c_double()
-    lib.gsks_probe_peak(0, C.byref(dfma))
-    fp64_peak = 2.0 * dfma.value  # flop/s
 
-    def one_call(ktype, params, u):
-        gsks.dgsks_device(kernel_desc(gsks, ktype, params), M_T, N_S, K_DIM, u, wl["umap"], wl["X"], wl["X2"],
-                          wl["amap"], wl["X"], wl["X2"], wl["bmap"], wl["w"], wl["wmap"], precision=prec,
-                          stream=stream, nxa=N_POOL, nxb=N_POOL)
-        return gsks.last_launch_count()
-
+def time_form(args, torch, gsks, wl, form, ws, flush, stream, clk):
+    """W warm-up + K timed steps of one form; per-kernel event times."""
+    prec = prec_of(gsks, form)
     u = torch.zeros(M_T, dtype=torch.float64, device="cuda")
     for _ in range(args.warmup):
         for _, kt, p, _f in KERNELS:
-            one_call(kt, p, u)
+            device_call(gsks, wl, kt, p, u, prec, stream)
     torch.cuda.synchronize()
-
     evs = {name: [] for name, *_ in KERNELS}
     launches = 0
     barrier(ws)
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
+    with clk:
+        t0 = torch.cuda.Event(enable_timing=True); t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
-        for s in range(args.steps):
+        for _ in range(args.steps):
             flush.zero_()
+            launches += 1
             for name, kt, p, _f in KERNELS:
                 a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
                 a.record(stream)
-                launches += one_call(kt, p, u)
+                launches += device_call(gsks, wl, kt, p, u, prec, stream)
                 b.record(stream)
                 evs[name].append((a, b))
-            launches += 1  # the L2 flush memset
         t1.record(stream)
         torch.cuda.synchronize()
     barrier(ws)
-    ms_local = t0.elapsed_time(t1)
-    ms = max_over_ranks(ws, ms_local)
-    pairs_step = len(KERNELS) * M_T * N_S
-    value = pairs_step * args.steps * ws / (ms * 1e-3)
+    ms = max_over_ranks(ws, t0.elapsed_time(t1))
+    per = {name: statistics.mean(a.elapsed_time(b) for a, b in v) for name, v in evs.items()}
+    return ms, per, launches
 
-    # roofline per kernel type
-    per = {}
+
+def roofline_split(per, peaks, rates):
+    """Split form: algorithmic 2mnk at the tensor peak (and the executed split
+    products), ex2 at the measured SFU rate, per kernel."""
+    out = {}
+    tc_peak = peaks.get("bf16_tflops", 1900.0) * 1e12
+    for name, kt, p, _f in KERNELS:
+        t = per[name] * 1e-3
+        pairs = M_T * N_S
+        alg = 2.0 * pairs * K_DIM
+        execd = SPLIT_PRODUCTS * 2.0 * pairs * ((K_DIM + 15) // 16 * 16)
+        t_tc, t_exec = alg / tc_peak, execd / tc_peak
+        t_sfu = pairs / rates["ex2"] if kt in (0, 3) else 0.0
+        bound_t = max(t_tc, t_sfu)
+        out[name] = {"ms": round(per[name], 4), "pairs_per_s": pairs / t,
+                     "alg_tflops": round(alg / t / 1e12, 2), "frac_alg_tensor": round(t_tc / t, 4),
+                     "executed_tflops": round(execd / t / 1e12, 2), "frac_executed_tensor": round(t_exec / t, 4),
+                     "frac_sfu": round(t_sfu / t, 4) if t_sfu else None,
+                     "frac_of_binding": round(bound_t / t, 4)}
+    return out
+
+
+def roofline_fp64(per, rates):
+    out = {}
+    peak = 2.0 * rates["dfma"]
     for name, kt, p, f in KERNELS:
-        dur = statistics.mean(a.elapsed_time(b) for a, b in evs[name]) * 1e-3
+        t = per[name] * 1e-3
         flops = M_T * N_S * (2 * K_DIM + f)
-        per[name] = {"ms": dur * 1e3, "pairs_per_s": M_T * N_S / dur, "flops_alg": flops,
-                     "achieved_tflops": flops / dur / 1e12, "frac": flops / dur / fp64_peak}
-    dominant = max(per, key=lambda k: per[k]["ms"])
-    traffic = read_traffic(dominant)
-    roof = {"bound": "fp64", "kernel": f"fp64_tiles<{dominant}> + fp64_reduce",
-            "achieved": round(per[dominant]["achieved_tflops"], 4), "peak": round(fp64_peak / 1e12, 4),
-            "unit": "TFLOP/s", "frac": round(per[dominant]["frac"], 4), "traffic": traffic,
-            "peak_source": "measured live: gsks_probe_peak FP64 FMA issue rate x 2 (no FP64 entry in MEASURED_PEAKS.json)",
-            "flop_model": "m*n*(2k + f_type), f_type from test/test_dgsks.c:254-283",
-            "per_kernel": {k: {kk: (round(vv, 5) if isinstance(vv, float) else vv) for kk, vv in v.items()}
-                           for k, v in per.items()}}
-
-    line = {
-        "metric": METRIC, "value": value, "unit": "pair-evals/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16x3+f32+f64",
-        "data": "synthetic: seeded uniform[0,1]^64 pool, N(0,1) weights, random subset / permutation maps",
-        "config": {"workload": WORKLOAD, "precision": args.precision, "pool": N_POOL, "k": K_DIM,
-                   "m": M_T, "n": N_S, "kernels": [k[0] for k in KERNELS],
-                   "l2": "flushed between steps (512 MiB memset inside the timed region)",
-                   "parallelism": f"replicas x{ws}"},
-        "roofline": roof,
-        "gpu_launches": launches,
-        "clocks": clk.summary(),
-    }
-
-    # error of the GPU result on sampled rows + CPU baseline (rank 0, N=1 only)
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu, err = cpu_baseline_and_error(args, torch, gsks, wl, prec, stream)
-        line["cpu_baseline"] = cpu
-        line["error"] = err
-    if not args.no_e2e:
-        line["e2e"] = run_e2e(args, torch, gsks, wl, ws)
-    return line
+        out[name] = {"ms": round(per[name], 3), "pairs_per_s": M_T * N_S / t,
+                     "achieved_tflops": round(flops / t / 1e12, 4), "frac": round(flops / t / peak, 4)}
+    return out
 
 
-def read_traffic(kernel_name):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", f"fp64_tiles_{kernel_name}_c2.md")
+def read_traffic(name):
+    """DRAM bytes per launch from a committed ncu summary (profiles/<name>.md)."""
+    path = os.path.join(ROOT, "profiles", name + ".md")
     if not os.path.exists(path):
         return None
     for l in open(path):
@@ -308,36 +284,113 @@ def read_traffic(kernel_name):
     return None
 
 
-def run_e2e(args, torch, gsks, wl, ws):
-    """Same steps through ks.h dgsks() with host (numpy) arrays."""
+def run_ours(args, ws, rank, local):
+    import torch
+    from ks_gb300 import build as B
+    if not os.path.exists(B.LIB):
+        B.build()
+    from ks_gb300 import gsks
+    lib = gsks.load()
+    forms = [f for f in args.forms.split(",") if f]
+    wl = make_workload(torch)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    peaks = peaks_file()
+    rates = {}
+    for nm, w in (("dfma", 0), ("ffma", 1), ("ex2", 2)):
+        r = C.c_double()
+        lib.gsks_probe_peak(w, C.byref(r))
+        rates[nm] = r.value
+
+    clk = ClockSampler(local)
+    results = {}
+    for form in forms:
+        ms, per, launches = time_form(args, torch, gsks, wl, form, ws, flush, stream, clk)
+        pairs_step = len(KERNELS) * M_T * N_S
+        results[form] = {"value": pairs_step * args.steps * ws / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                         "gpu_launches": launches,
+                         "per_kernel": roofline_split(per, peaks, rates) if form == "split"
+                         else roofline_fp64(per, rates)}
+    head = forms[0]
+    H = results[head]
+
+    # top-level roofline: the headline form's dominant kernel
+    dom = max(H["per_kernel"], key=lambda k: H["per_kernel"][k]["ms"])
+    dk = H["per_kernel"][dom]
+    if head == "split":
+        t = dk["ms"] * 1e-3
+        roof = {"bound": "tensor", "kernel": f"split_tiles<{dom}>", "achieved": dk["alg_tflops"],
+                "peak": round(peaks.get("bf16_tflops", 1900.0), 1), "unit": "TFLOP/s",
+                "frac": dk["frac_alg_tensor"], "traffic": read_traffic(f"split_tiles_{dom}_c2"),
+                "flops": "algorithmic 2mnk per launch; the split form executes 6 f16 products per slice set "
+                         "(executed_tflops)",
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst; f16 runs at the bf16 rate)"
+                if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s bf16"}
+    else:
+        roof = {"bound": "fp64", "kernel": f"fp64_tiles<{dom}>", "achieved": dk["achieved_tflops"],
+                "peak": round(2 * rates["dfma"] / 1e12, 4), "unit": "TFLOP/s", "frac": dk["frac"],
+                "traffic": read_traffic(f"fp64_tiles_{dom}_c2"),
+                "peak_source": "measured live: gsks_probe_peak FP64 FMA rate x 2"}
+    roof["per_form"] = {f: results[f]["per_kernel"] for f in forms}
+    roof["pipe_rates_measured"] = {k: float("%.4g" % v) for k, v in rates.items()}
+
+    line = {
+        "metric": METRIC, "value": H["value"], "unit": "pair-evals/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": H["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f16x3 split + f32 kernel + f64 sums" if head == "split" else "f64",
+        "data": "synthetic: seeded uniform[0,1]^64 pool, N(0,1) weights, random subset / permutation maps",
+        "config": {"workload": WORKLOAD, "form": head, "pool": N_POOL, "k": K_DIM, "m": M_T, "n": N_S,
+                   "kernels": [k[0] for k in KERNELS],
+                   "l2": "flushed between steps (512 MiB memset inside the timed region)",
+                   "parallelism": f"replicas x{ws}"},
+        "forms": {f: {"value": results[f]["value"], "ms_per_step": results[f]["ms_per_step"]} for f in forms},
+        "roofline": roof,
+        "gpu_launches": H["gpu_launches"],
+        "clocks": clk.summary(),
+    }
+    if "split" in results and "fp64" in results:
+        line["forms"]["split_over_fp64"] = results["split"]["value"] / results["fp64"]["value"]
+
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu, err = cpu_baseline_and_error(args, torch, gsks, wl, forms, stream)
+        line["cpu_baseline"] = cpu
+        line["error"] = err
+    if not args.no_e2e:
+        line["e2e"] = run_e2e(args, torch, gsks, wl, ws, head)
+    return line
+
+
+def run_e2e(args, torch, gsks, wl, ws, form):
+    """The same steps through ks.h dgsks() with host (numpy) arrays."""
     import numpy as np
     h = {k: v.cpu().numpy() for k, v in wl.items()}
+    gsks.set_precision(prec_of(gsks, form))
     u = np.zeros(M_T)
-    steps = max(1, args.steps)
-    for _ in range(1):
-        for _, kt, p, _f in KERNELS:
-            rc = gsks.dgsks_status(kernel_desc(gsks, kt, p), u, h["umap"], h["X"], h["X2"], h["amap"], h["X"],
-                                   h["X2"], h["bmap"], h["w"], h["wmap"])
-            assert rc == 0, gsks.error_string(rc)
+    for _, kt, p, _f in KERNELS:   # one warm-up step
+        rc = gsks.dgsks_status(gsks.make_kernel(kt, **p), u, h["umap"], h["X"], h["X2"], h["amap"], h["X"],
+                               h["X2"], h["bmap"], h["w"], h["wmap"])
+        assert rc == 0, gsks.error_string(rc)
     barrier(ws)
+    steps = max(1, args.steps)
     t0 = time.perf_counter()
     for _ in range(steps):
         for _, kt, p, _f in KERNELS:
-            gsks.dgsks_status(kernel_desc(gsks, kt, p), u, h["umap"], h["X"], h["X2"], h["amap"], h["X"],
+            gsks.dgsks_status(gsks.make_kernel(kt, **p), u, h["umap"], h["X"], h["X2"], h["amap"], h["X"],
                               h["X2"], h["bmap"], h["w"], h["wmap"])
     dt = max_over_ranks(ws, time.perf_counter() - t0)
+    gsks.set_precision(gsks.GSKS_FP64)
     # bytes the host path copies per call: gathered A and B rows, norms, w, u in; u out
-    h2d_call = 8 * (M_T * K_DIM + N_S * K_DIM + M_T + N_S + N_S + M_T)
-    h2d_poly = 8 * (M_T * K_DIM + N_S * K_DIM + N_S + M_T)  # no norms for the inner-product kernel
-    h2d = 2 * h2d_call + h2d_poly
-    return {"value": len(KERNELS) * M_T * N_S * steps * ws / dt, "unit": "pair-evals/s",
-            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 8 * M_T * len(KERNELS),
+    h2d_norm = 8 * (M_T * K_DIM + N_S * K_DIM + M_T + N_S + N_S + M_T)
+    h2d_ip = 8 * (M_T * K_DIM + N_S * K_DIM + N_S + M_T)   # the inner-product kernel sends no norms
+    return {"value": len(KERNELS) * M_T * N_S * steps * ws / dt, "unit": "pair-evals/s", "form": form,
+            "h2d_bytes_per_step": 2 * h2d_norm + h2d_ip, "d2h_bytes_per_step": 8 * M_T * len(KERNELS),
             "path": "ks.h dgsks() with host numpy arrays (pinned staging inside the call)"}
 
 
-def cpu_baseline_and_error(args, torch, gsks, wl, prec, stream):
+def cpu_baseline_and_error(args, torch, gsks, wl, forms, stream):
     """CPU port of the reference's fused dgsks on sampled rows x all sources, all
-    host cores; the same row sums measure the GPU result's error."""
+    host cores; the same row sums give each GPU form's error on those rows."""
     import numpy as np
     from oracle import oracle as O
     O.build()
@@ -348,32 +401,31 @@ def cpu_baseline_and_error(args, torch, gsks, wl, prec, stream):
     # that coincident pool points cancel exactly there (Laplace is singular at
     # d2 = 0, frame/dgsks_ref.c:343-345); the GPU used its device-computed norms.
     h["X2"] = O.norms(h["X"])
-    # one fresh GPU evaluation of each kernel into its own u for the comparison
     gpu_u = {}
-    for name, kt, p, _f in KERNELS:
-        u = torch.zeros(M_T, dtype=torch.float64, device="cuda")
-        gsks.dgsks_device(kernel_desc(gsks, kt, p), M_T, N_S, K_DIM, u, wl["umap"], wl["X"], wl["X2"], wl["amap"],
-                          wl["X"], wl["X2"], wl["bmap"], wl["w"], wl["wmap"], precision=prec, stream=stream)
-        torch.cuda.synchronize()
-        gpu_u[name] = u.cpu().numpy()
-    # calibrate the sample to about args.cpu_seconds of CPU work
+    for form in forms:
+        for name, kt, p, _f in KERNELS:
+            u = torch.zeros(M_T, dtype=torch.float64, device="cuda")
+            device_call(gsks, wl, kt, p, u, prec_of(gsks, form), stream)
+            torch.cuda.synchronize()
+            gpu_u[(form, name)] = u.cpu().numpy()
     rng = np.random.default_rng(7)
+
     def timed(rows):
-        t = 0.0
-        outs = {}
+        t, outs = 0.0, {}
         for name, kt, p, _f in KERNELS:
             amap_s = np.ascontiguousarray(h["amap"][rows])
-            umap_s = np.arange(rows.size, dtype=np.int32)
             u_s = np.zeros(rows.size)
             t0 = time.perf_counter()
-            O.dgsks(O.make_kernel(kt, **p), u_s, umap_s, h["X"], h["X2"], amap_s, h["X"], h["X2"], h["bmap"],
-                    h["w"], h["wmap"], impl="fused")
+            O.dgsks(O.make_kernel(kt, **p), u_s, np.arange(rows.size, dtype=np.int32), h["X"], h["X2"], amap_s,
+                    h["X"], h["X2"], h["bmap"], h["w"], h["wmap"], impl="fused")
             t += time.perf_counter() - t0
             outs[name] = u_s
         return t, outs
-    rows0 = np.sort(rng.choice(M_T, 64, replace=False)).astype(np.int32)
+
+    timed(np.arange(16, dtype=np.int32))                       # thread start-up
+    rows0 = np.sort(rng.choice(M_T, 128, replace=False)).astype(np.int32)
     t0, _ = timed(rows0)
-    S = int(min(M_T, max(64, 64 * args.cpu_seconds / max(t0, 1e-3))))
+    S = int(min(M_T, max(128, 128 * args.cpu_seconds / max(t0, 1e-3))))
     rows = np.sort(rng.choice(M_T, S, replace=False)).astype(np.int32)
     t, outs = timed(rows)
     pairs = len(KERNELS) * S * N_S
@@ -382,21 +434,21 @@ def cpu_baseline_and_error(args, torch, gsks, wl, prec, stream):
                      f"({pairs:.3g} pairs, {t:.1f} s)",
            "impl": "oracle_dgsks_fused (C restatement of frame/dgsks.c, OpenMP); the reference's AVX "
                    "micro-kernels do not build on aarch64"}
-    err = {}
-    for name, kt, p, _f in KERNELS:
-        _, cond = O.rows(O.make_kernel(kt, **p), rows, h["X"], h["X2"], h["amap"], h["X"], h["X2"], h["bmap"],
-                         h["w"], h["wmap"])
-        ug = gpu_u[name][h["umap"][rows]]
-        e = O.errors(ug, outs[name], cond=cond)
-        err[name] = {k: float("%.3g" % v) for k, v in e.items()}
-    err["rows_checked"] = int(S)
+    err = {"rows_checked": int(S),
+           "metrics": "normwise ||du||/||u||; cond = max_i |du_i| / sum_j |K_ij w_j|"}
+    for form in forms:
+        err[form] = {}
+        for name, kt, p, _f in KERNELS:
+            _, cond = O.rows(O.make_kernel(kt, **p), rows, h["X"], h["X2"], h["amap"], h["X"], h["X2"],
+                             h["bmap"], h["w"], h["wmap"])
+            e = O.errors(gpu_u[(form, name)][h["umap"][rows]], outs[name], cond=cond)
+            err[form][name] = {k: float("%.3g" % v) for k, v in e.items()}
     return cpu, err
 
 
 def run_reference(args, ws, rank):
     """The reference's CPU implementation of the path on this host's cores: the
-    oracle port of its fused dgsks (the reference's AVX micro-kernels do not
-    build on aarch64), bounded sample per step."""
+    oracle port of its fused dgsks, bounded sample of target rows per step."""
     import numpy as np
     if rank != 0:
         return None
@@ -418,22 +470,22 @@ def run_reference(args, ws, rank):
             u = np.zeros(S)
             O.dgsks(O.make_kernel(kt, **p), u, np.arange(S, dtype=np.int32), X, X2,
                     np.ascontiguousarray(amap[rows]), X, X2, bmap, w, wmap, impl="fused")
-    t0 = time.perf_counter(); step(32); t1 = time.perf_counter() - t0
-    budget = 120.0 / max(1, args.steps + args.warmup)   # whole run within a few minutes
-    S = int(min(M_T, max(32, 32 * min(budget, 15.0) / max(t1, 1e-3))))
+    step(16)
+    t0 = time.perf_counter(); step(128); t1 = time.perf_counter() - t0
+    budget = min(15.0, 120.0 / max(1, args.steps + args.warmup))   # whole run within a few minutes
+    S = int(min(M_T, max(64, 128 * budget / max(t1, 1e-3))))
     for _ in range(args.warmup):
         step(S)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step(S)
     dt = time.perf_counter() - t0
-    pairs = len(KERNELS) * S * N_S * args.steps
-    v = pairs / dt
+    v = len(KERNELS) * S * N_S * args.steps / dt
     return {"metric": METRIC, "value": v, "unit": "pair-evals/s", "impl": "reference", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: seeded uniform[0,1]^64 pool, N(0,1) weights",
-            "config": {"workload": WORKLOAD, "precision": "fp64", "sample_rows_per_step": S},
+            "config": {"workload": WORKLOAD, "form": "cpu fp64", "sample_rows_per_step": S},
             "cpu_baseline": {"value": v, "unit": "pair-evals/s", "cores": cores, "kind": "port",
                              "sample": f"{S} random target rows x all {N_S} sources x {len(KERNELS)} kernels per step"},
             "e2e": {"value": v, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -450,7 +502,7 @@ def main():
         if line is not None:
             print(json.dumps(line), flush=True)
         return
-    ws, rank, local = dist_setup(args)
+    ws, rank, local = dist_setup()
     line = run_ours(args, ws, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -268,8 +268,8 @@ KParams make_kparams(const ks_t *ker, const double *hi, const double *hj)
   kp.coinc = 0.0;
   kp.pmode = POW_GENERAL; kp.pint = 0;
   const double p = ker->powe;
-  if (fabs(p) <= 64.0 && p == rint(p)) { kp.pmode = POW_INT; kp.pint = (int)p; }
-  else if (fabs(p) <= 64.0 && 2.0 * p == rint(2.0 * p)) { kp.pmode = POW_HALF; kp.pint = (int)floor(p); }
+  if (fabs(p) <= 511.0 && p == rint(p)) { kp.pmode = POW_INT; kp.pint = (int)p; }
+  else if (fabs(p) <= 511.0 && 2.0 * p == rint(2.0 * p)) { kp.pmode = POW_HALF; kp.pint = (int)floor(p); }
   return kp;
 }
 

@@ -29,7 +29,7 @@ struct KParams {
   // reference's coincident-point clamp (frame/dgsks_ref.c:343-345).
   double coinc;
   // Exponent class of powe (polynomial, Laplace): integer and half-integer
-  // exponents up to 64 in magnitude are evaluated by binary powering (and one
+  // exponents up to 511 in magnitude are evaluated by binary powering (and one
   // square root) instead of the general pow().
   int pmode, pint;
 };

@@ -58,7 +58,7 @@ constexpr int BN = 128;             // sources per tile
 constexpr int KPAD_MAX = 64;        // padded k of the target-resident kernel
 constexpr int NSTAGE = 2;           // source-tile stages
 constexpr int NBLK = 3;             // slices per operand
-constexpr int EPI_WARPS = 4;
+constexpr int EPI_WARPS = 8;
 constexpr int NTHREADS = 32 * (2 + EPI_WARPS);
 constexpr long long WAIT_LIMIT = 1LL << 32;   // clock cycles (~2 s) per wait
 constexpr uint32_t TMEM_COLS = 512;           // 2 buffers x (H, L) x 128 columns
@@ -77,6 +77,9 @@ struct Params {          // per call, computed on the device
   float t_flag;          // flag pairs with t < t_flag ...
   float rho;             // ... or t < rho * (n_i + n_j)
   int centred;
+  int any_flag;          // some pair may be flagged
+  int exact_t1;          // n_i + n_j - 2 sigma^2 2^-14 H is exact in FP32
+  float c0h, c0l;        // Laplace: scal^(1/m), m = -powe, as a double-float
 };
 
 __host__ __device__ inline size_t blk_bytes(int rows, int kpad) { return (size_t)rows * kpad * 2; }
@@ -171,8 +174,10 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     P->centred = dist ? 1 : 0;
     // Absolute error bound of the assembled d2 (in the scaled units): rounding
     // of the L accumulator and of the split norms, plus the slicing remainder.
-    const double delta = 4.0 * (sigma * sigma * (double)k * 0x1p-31) +
-                         4.0 * sigma * sqrt((double)k) * sqrt(nbound) * 0x1p-30 + 2.0 * q * 0x1p-23;
+    // (Calibrated: over a 16384-pair tile at k = 64, sigma = 1, the largest
+    // |t + lo - d2| was 1.4e-7, and this expression gives 1.6e-7 there.)
+    const double delta = 2.0 * (sigma * sigma * (double)k * 0x1p-31) +
+                         2.0 * sigma * sqrt((double)k) * sqrt(nbound) * 0x1p-30 + 2.0 * q * 0x1p-23;
     float t_flag = -1.0f, rho = 0.0f;
     if (kt == KS_GAUSSIAN) {
       // relative error of 2^-d2 is ln2 * delta; pairs with t >= 126 underflow anyway
@@ -182,10 +187,20 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     } else if (kt == KS_LAPLACE) {
       rho = 0x1p-10f;                         // coincident points and near-cancellation
       t_flag = (float)(fabs(powe) * delta / tau);
+      // (c0 / d2)^m stays below 2^120 for d2 above c0 2^(-120/m)
+      const double mm = -powe, c0 = pow(scal, 1.0 / mm);
+      P->c0h = (float)c0;
+      P->c0l = (float)(c0 - (double)P->c0h);
+      t_flag = fmaxf(t_flag, (float)(c0 * exp2(-120.0 / mm) * 1.001));
     } else if (dist) {
       rho = 0.0f;                             // compact / polynomial in d2: absolute error only
     }
     P->t_flag = t_flag; P->rho = rho;
+    P->any_flag = (t_flag > 0.0f || rho > 0.0f) ? 1 : 0;
+    // |x''|^2 + |y''|^2 lies on the grid q and -2 sigma^2 2^-14 H on the grid
+    // 2 sigma^2 2^-14; when the latter is a multiple of q their sum is exact
+    // (it stays below 2^24 q), and only the small L term needs Fast2Sum.
+    P->exact_t1 = (q <= 2.0 * sigma * sigma * 0x1p-14) ? 1 : 0;
   }
 }
 
@@ -281,7 +296,34 @@ struct SplitSmem {
   uint32_t tmem_base;
   int abort;
   int never;             // stays 0: an abort flag for the drain waits
+  double rsum[2][BM];    // row sums of epilogue group 1, by item parity
 };
+
+// Double-float (unevaluated FP32 pair) product, a *= b: Dekker's product with
+// the FMA giving the exact error of the high product.
+__device__ __forceinline__ void df_mul(float &ah, float &al, float bh, float bl)
+{
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  const float s = p + e;
+  al = e - (s - p);
+  ah = s;
+}
+
+// Double-float reciprocal, a = 1 / a, one Newton step on the FP32 quotient.
+__device__ __forceinline__ void df_rcp(float &ah, float &al)
+{
+  float q = rcp_approx(ah);
+  q = fmaf(q, fmaf(-ah, q, 1.0f), q);        // Newton step: q to ~1 ulp of 1/ah
+  float r = fmaf(-ah, q, 1.0f);
+  r = fmaf(-al, q, r);
+  const float ql = q * r;
+  const float s = q + ql;
+  al = ql - (s - q);
+  ah = s;
+}
 
 // FP32 kernel value from the double-float squared distance t + lo (scaled
 // units) or, for inner-product kernels, from c = x.y.
@@ -308,17 +350,27 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
     }
     return ex2_approx((float)kp.powe * __log2f(v));
   } else if constexpr (KT == KS_LAPLACE) {
-    const float d = t + lo;
-    if (kp.pmode == POW_INT || kp.pmode == POW_HALF) {
-      // d^powe = d^pint (x sqrt(d) for half-integers), binary powering
-      int e = kp.pint < 0 ? -kp.pint : kp.pint;
-      float r = 1.0f, b = d;
-      for (;;) { if (e & 1) r *= b; e >>= 1; if (!e) break; b *= b; }
-      float v = kp.pint < 0 ? 1.0f / r : r;
-      if (kp.pmode == POW_HALF) v *= sqrtf(d);
-      return (float)kp.scal * v;
+    // scal * d2^powe with powe = -m < 0 (k >= 3), evaluated as (c0 / d2)^m with
+    // c0 = scal^(1/m): the intermediates stay in the FP32 range for every d2
+    // whose kernel value does (smaller d2 are flagged and done in FP64).  The
+    // base is a double-float through binary powering: m up to 32 would
+    // amplify a single FP32 rounding of d2 m-fold.  hrow / hcol carry c0.
+    float bh = t, bl = lo;
+    df_rcp(bh, bl);
+    df_mul(bh, bl, hrow, hcol);
+    const int m = -kp.pint - (kp.pmode == POW_HALF ? 1 : 0);   // integer part of -powe
+    float rh = 1.0f, rl = 0.0f, ph = bh, pl = bl;
+#pragma unroll
+    for (int bit = 0; bit < 9; bit++) {      // fixed trip count (m < 512), uniform branches
+      if (m & (1 << bit)) df_mul(rh, rl, ph, pl);
+      if (m >> (bit + 1)) df_mul(ph, pl, ph, pl);
     }
-    return (float)kp.scal * ex2_approx((float)kp.powe * __log2f(d));
+    if (kp.pmode == POW_HALF) {
+      const float sh = sqrtf(bh);
+      const float sl = (fmaf(-sh, sh, bh) + bl) / (2.0f * sh);   // sqrt(bh + bl) = sh + sl
+      df_mul(rh, rl, sh, sl);
+    }
+    return rh + rl;
   } else if constexpr (KT == KS_TANH) {
     const float v = fmaf((float)kp.scal, c, (float)kp.cons);
     const float av = fabsf(v);
@@ -367,6 +419,91 @@ __device__ double recheck64(const TileArgs &a, int ipos, int jpos)
   else if constexpr (KT == KS_EPANECHNIKOV) kv = d2 < 1.0 ? 0.75 * (1.0 - d2) : 0.0;
   else kv = 0.0;
   return kv * wv;
+}
+
+// Squared distance t + lo (double-float, scaled units) of one pair from its
+// accumulators and split norms.
+template <bool EXACT>
+__device__ __forceinline__ void assemble(float H, float L, float an_hi, float an_lo, float bn_hi, float bn_lo,
+                                         float rc, float &t, float &lo, float &s)
+{
+  s = an_hi + bn_hi;                          // exact on the grid q
+  const float pL = L * rc, pH = H * rc;       // exact (rc is a power of 2)
+  if constexpr (EXACT) {
+    const float t1 = s + pH;                  // exact: both on the grid q, |t1| < 2^24 q
+    t = t1 + pL;
+    lo = (an_lo + bn_lo) + (pL - (t - t1));   // Fast2Sum
+  } else {
+    const float u1 = s + pL;
+    const float e1 = pL - (u1 - s);           // Fast2Sum: |s| >= |pL|
+    t = u1 + pH;
+    const float e2 = pH - (t - u1);           // Fast2Sum: |u1| >= |pH|
+    lo = ((an_lo + bn_lo) + e1) + e2;
+  }
+}
+
+// 32 columns of one row, distance kernels.  Returns the flagged columns.
+template <int KT, bool EXACT, bool FLAGS>
+__device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[32], const uint32_t (&l)[32],
+                                              const PtMeta *__restrict__ bm, const PtMeta &am, float rc,
+                                              const Params *P, const KParams &kp, float (&acc)[4])
+{
+  uint32_t flags = 0;
+  float t_flag = 0.f, rho = 0.f;
+  if constexpr (FLAGS) { t_flag = P->t_flag; rho = P->rho; }
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    const float4 m0 = *(const float4 *)&bm[j];   // n_hi, n_lo, w, h
+    float t, lo, s;
+    assemble<EXACT>(__uint_as_float(h[j]), __uint_as_float(l[j]), am.n_hi, am.n_lo, m0.x, m0.y, rc, t, lo, s);
+    float kv;
+    if constexpr (KT == KS_LAPLACE) kv = kval32<KT>(t, lo, 0.f, P->c0h, P->c0l, kp);
+    else kv = kval32<KT>(t, lo, 0.f, am.h, m0.w, kp);
+    if constexpr (FLAGS) {
+      if (t < t_flag || t < rho * s) { flags |= 1u << j; kv = 0.f; }
+    }
+    // padding columns carry w = 0 and finite distances
+    acc[j & 3] = fmaf(kv, m0.z, acc[j & 3]);
+  }
+  return flags;
+}
+
+// 32 columns of one row, inner-product kernels (polynomial, tanh).
+template <int KT>
+__device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[32], const uint32_t (&l)[32],
+                                             const PtMeta *__restrict__ bm, int valid, float rc,
+                                             const KParams &kp, float (&acc)[4])
+{
+#pragma unroll
+  for (int j = 0; j < 32; j++) {
+    const float w = bm[j].w;
+    const float cc = fmaf(__uint_as_float(l[j]), rc, __uint_as_float(h[j]) * rc) * -0.5f;  // x.y
+    const float kv = kval32<KT>(0.f, 0.f, cc, 0.f, 0.f, kp);
+    acc[j & 3] += (j < valid) ? kv * w : 0.f;      // the kernel of a padding column may be NaN
+  }
+}
+
+// Test hook: raw accumulators and epilogue values of 32 columns.
+template <int KT>
+__device__ void dump_chunk(float *dump, int row, int ch, const uint32_t (&h)[32], const uint32_t (&l)[32],
+                           const PtMeta *bm, const PtMeta &am, float rc, const KParams &kp)
+{
+  for (int j = 0; j < 32; j++) {
+    const int c = ch * 32 + j;
+    float *dp = dump + ((size_t)row * BN + c) * 5;
+    const float H = __uint_as_float(h[j]), L = __uint_as_float(l[j]);
+    dp[0] = H; dp[1] = L;
+    if constexpr (kt_uses_norms(KT)) {
+      float t, lo, s;
+      assemble<false>(H, L, am.n_hi, am.n_lo, bm[j].n_hi, bm[j].n_lo, rc, t, lo, s);
+      dp[2] = 0.f;
+      if constexpr (KT != KS_LAPLACE) dp[2] = kval32<KT>(t, lo, 0.f, am.h, bm[j].h, kp);
+      dp[3] = t; dp[4] = lo;
+    } else {
+      dp[2] = kval32<KT>(0.f, 0.f, fmaf(L, rc, H * rc) * -0.5f, 0.f, 0.f, kp);
+      dp[3] = dp[4] = 0.f;
+    }
+  }
 }
 
 template <int KT>
@@ -472,10 +609,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       mbar_wait(&S->drain, 0, &S->never, 1LL << 30);
     }
   } else {
-    // ---------------- epilogue (warps 2..5) ----------------
-    const int qd = warp & 3;               // TMEM sub-partition of this warp
+    // ---------------- epilogue (warps 2 .. 2+EPI_WARPS-1) ----------------
+    // Two groups of four warps; group g takes columns [64g, 64g+64) of every
+    // tile, each warp the 32 TMEM lanes (= target rows) of its sub-partition.
+    const int ew = warp - 2;
+    const int grp = ew >> 2;
+    const int qd = warp & 3;
     const int row = qd * 32 + lane;
-    const float rc = a.P->rc, t_flag = a.P->t_flag, rho = a.P->rho;
+    const Params *P = a.P;
+    const float rc = P->rc;
+    const bool flags_on = P->any_flag != 0, exact = P->exact_t1 != 0;
     int g = 0, tc = 0;
     for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
       const int ti = item % a.ntm, sc = item / a.ntm;
@@ -493,51 +636,23 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         tc_fence_after();
         const PtMeta *bm = (const PtMeta *)(sB + st * b_stride + NBLK * blk_bytes(BN, kpad));
         const int ncols = min(BN, a.n - tj * BN);
-        float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
         const uint32_t tH = tmem + ((uint32_t)(qd * 32) << 16) + buf * 256;
 #pragma unroll 1
-        for (int ch = 0; ch < BN / 32; ch++) {
+        for (int ch = 2 * grp; ch < 2 * grp + 2; ch++) {
           uint32_t h[32], l[32];
           tmem_ld32(tH + ch * 32, h);
           tmem_ld32(tH + 128 + ch * 32, l);
           tmem_ld_wait();
           uint32_t flags = 0;
-#pragma unroll
-          for (int j = 0; j < 32; j++) {
-            const int c = ch * 32 + j;
-            const PtMeta bj = bm[c];
-            const float H = __uint_as_float(h[j]), L = __uint_as_float(l[j]);
-            float kv;
-            if constexpr (kt_uses_norms(KT)) {
-              const float s = am.n_hi + bj.n_hi;            // exact on the grid q
-              const float pL = L * rc, pH = H * rc;         // exact (rc is a power of 2)
-              const float u1 = s + pL;
-              const float e1 = pL - (u1 - s);               // Fast2Sum: |s| >= |pL|
-              const float t = u1 + pH;
-              const float e2 = pH - (t - u1);               // Fast2Sum: |u1| >= |pH|
-              const float lo = ((am.n_lo + bj.n_lo) + e1) + e2;   // rounding residue only
-              kv = kval32<KT>(t, lo, 0.f, am.h, bj.h, a.kp);
-              if (t < t_flag || t < rho * s) { flags |= 1u << j; kv = 0.f; }
-            } else {
-              const float cc = fmaf(L, rc, H * rc) * -0.5f;  // x.y = sigma^2 2^-14 (H + L)
-              kv = kval32<KT>(0.f, 0.f, cc, 0.f, 0.f, a.kp);
-            }
-            if (a.dump && blockIdx.x == 0 && tc == 0) {
-              float *dp = a.dump + ((size_t)row * BN + c) * 5;
-              dp[0] = H; dp[1] = L; dp[2] = kv;
-              if constexpr (kt_uses_norms(KT)) {
-                const float s = am.n_hi + bj.n_hi, pL = L * rc, pH = H * rc;
-                const float u1 = s + pL, t = u1 + pH;
-                dp[3] = t; dp[4] = ((am.n_lo + bj.n_lo) + (pL - (u1 - s))) + (pH - (t - u1));
-              }
-            }
-            const float term = (c < ncols) ? kv * bj.w : 0.f;
-            if ((j & 3) == 0) acc0 += term;
-            else if ((j & 3) == 1) acc1 += term;
-            else if ((j & 3) == 2) acc2 += term;
-            else acc3 += term;
-          }
           if constexpr (kt_uses_norms(KT)) {
+            if (exact) {
+              if (flags_on) flags = epi_chunk<KT, true, true>(h, l, bm + ch * 32, am, rc, P, a.kp, acc);
+              else epi_chunk<KT, true, false>(h, l, bm + ch * 32, am, rc, P, a.kp, acc);
+            } else {
+              if (flags_on) flags = epi_chunk<KT, false, true>(h, l, bm + ch * 32, am, rc, P, a.kp, acc);
+              else epi_chunk<KT, false, false>(h, l, bm + ch * 32, am, rc, P, a.kp, acc);
+            }
             // FP64 rechecks of the flagged pairs of this 32-column chunk
             while (flags) {
               const int j = __ffs(flags) - 1;
@@ -545,16 +660,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
               const int c = ch * 32 + j;
               if (c < ncols && am.pos >= 0) racc += recheck64<KT>(a, am.pos, bm[c].pos);
             }
+          } else {
+            epi_chunk_ip<KT>(h, l, bm + ch * 32, ncols - ch * 32, rc, a.kp, acc);
           }
+          if (a.dump && blockIdx.x == 0 && tc == 0) dump_chunk<KT>(a.dump, row, ch, h, l, bm + ch * 32, am, rc, a.kp);
         }
-        racc += ((double)acc0 + (double)acc1) + ((double)acc2 + (double)acc3);
+        racc += ((double)acc[0] + (double)acc[1]) + ((double)acc[2] + (double)acc[3]);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) { mbar_arrive(&S->t_empty[buf]); mbar_arrive(&S->b_empty[st]); }
       }
       if (!ok) break;
-      const int grow = ti * BM + row;
-      if (grow < a.m) a.partial[(size_t)sc * a.ldp + grow] = racc;
+      // combine the two column groups' row sums (double-buffered by item parity)
+      double *xs = S->rsum[it & 1];
+      if (grp == 1) xs[row] = racc;
+      asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");
+      if (grp == 0) {
+        const int grow = ti * BM + row;
+        if (grow < a.m) a.partial[(size_t)sc * a.ldp + grow] = racc + xs[row];
+      }
     }
   }
 
