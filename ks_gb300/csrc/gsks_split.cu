@@ -56,9 +56,11 @@ using namespace sm100;
 constexpr int BM = 128;             // targets per tile (TMEM lanes)
 constexpr int BN = 128;             // sources per tile
 constexpr int KPAD_MAX = 64;        // padded k of the target-resident kernel
-constexpr int NSTAGE = 2;           // source-tile stages
+constexpr int NSTAGE = 3;           // source-tile operand stages
+constexpr int NMETA = 4;            // source-tile metadata ring
 constexpr int NBLK = 3;             // slices per operand
-constexpr int EPI_WARPS = 8;
+constexpr int EPI_GROUPS = 4;          // column groups of the epilogue
+constexpr int EPI_WARPS = 4 * EPI_GROUPS;
 constexpr int NTHREADS = 32 * (2 + EPI_WARPS);
 constexpr long long WAIT_LIMIT = 1LL << 32;   // clock cycles (~2 s) per wait
 constexpr uint32_t TMEM_COLS = 512;           // 2 buffers x (H, L) x 128 columns
@@ -73,12 +75,14 @@ struct PtMeta {          // 32 bytes per point, appended to each tile image
 
 struct Params {          // per call, computed on the device
   double alpha, sigma, inv_sigma, q;
-  float rc;              // -2 sigma^2 2^-14: multiplies H and L
+  double g;              // 2 sigma^2 2^-14: d2 = g (nu_i + nu_j - H - L)
+  float rc;              // -g as a float
   float t_flag;          // flag pairs with t < t_flag ...
   float rho;             // ... or t < rho * (n_i + n_j)
   int centred;
   int any_flag;          // some pair may be flagged
-  int exact_t1;          // n_i + n_j - 2 sigma^2 2^-14 H is exact in FP32
+  int exact_t1;          // nu_i + nu_j - H is exact in FP32
+  int gfast;             // Gaussian without flags: low norm parts folded into w / row factors
   float c0h, c0l;        // Laplace: scal^(1/m), m = -powe, as a double-float
 };
 
@@ -170,7 +174,8 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     const double nbound = alpha * alpha * s_sq[0];        // >= any |x''|^2
     const double q = exp2(ceil(log2(2.0 * nbound + 1e-300)) - 23.0);
     P->alpha = alpha; P->sigma = sigma; P->inv_sigma = 1.0 / sigma; P->q = q;
-    P->rc = (float)(-2.0 * sigma * sigma * 0x1p-14);
+    P->g = 2.0 * sigma * sigma * 0x1p-14;
+    P->rc = (float)(-P->g);
     P->centred = dist ? 1 : 0;
     // Absolute error bound of the assembled d2 (in the scaled units): rounding
     // of the L accumulator and of the split norms, plus the slicing remainder.
@@ -201,6 +206,7 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     // 2 sigma^2 2^-14; when the latter is a multiple of q their sum is exact
     // (it stays below 2^24 q), and only the small L term needs Fast2Sum.
     P->exact_t1 = (q <= 2.0 * sigma * sigma * 0x1p-14) ? 1 : 0;
+    P->gfast = (kt == KS_GAUSSIAN && P->exact_t1 && !P->any_flag) ? 1 : 0;
   }
 }
 
@@ -253,15 +259,28 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
     *(uint4 *)(base + 1 * bb + off) = *(const uint4 *)s2;
     *(uint4 *)(base + 2 * bb + off) = *(const uint4 *)s3;
   }
-  nrm *= P->sigma * P->sigma;                          // back to the x'' units
+  // The norm in units of the accumulators: nu = |x''|^2 / g with
+  // g = 2 sigma^2 2^-14, so that d2 = g (nu_i + nu_j - H - L).  nu is split on
+  // the grid q / g (a power of two): its high parts and H add exactly.
+  const double g = P->g;
+  const double nu = nrm * (P->sigma * P->sigma) / g;
+  const double qg = P->q / g;
+  const double nh = rint(nu / qg) * qg;
+  const double nl = nu - nh;
   PtMeta mt;
-  const double q = P->q;
-  const double nh = rint(nrm / q) * q;
   mt.n_hi = (float)nh;
-  mt.n_lo = (float)(nrm - nh);
+  mt.n_lo = (float)nl;
   mt.w = 0.0f;
   mt.h = 0.0f;
   if (side == 1 && valid) mt.w = (float)w[wmap ? wmap[pt] : pt];
+  if (P->gfast) {
+    // Gaussian: 2^-(g nl) is a per-point factor; fold it into w for sources
+    // and into a row factor for targets (applied to the row sum)
+    const double f = exp2(-g * nl);
+    mt.n_lo = 0.0f;
+    if (side == 1) mt.w = valid ? (float)(w[wmap ? wmap[pt] : pt] * f) : 0.0f;
+    else mt.h = (float)f;
+  }
   if (kt == KS_GAUSSIAN_VAR_BANDWIDTH && valid) {
     const double hv = hvec[pidx];
     mt.h = side == 0 ? (float)(-0.5 * 1.4426950408889634 * hv) : (float)hv;
@@ -291,12 +310,13 @@ struct TileArgs {
 struct SplitSmem {
   uint64_t a_full, a_empty;
   uint64_t b_full[NSTAGE], b_empty[NSTAGE];
+  uint64_t m_full[NMETA], m_empty[NMETA];
   uint64_t t_full[2], t_empty[2];
   uint64_t drain;
   uint32_t tmem_base;
   int abort;
   int never;             // stays 0: an abort flag for the drain waits
-  double rsum[2][BM];    // row sums of epilogue group 1, by item parity
+  double rsum[2][EPI_GROUPS - 1][BM];   // row sums of epilogue groups 1.., by item parity
 };
 
 // Double-float (unevaluated FP32 pair) product, a *= b: Dekker's product with
@@ -423,28 +443,55 @@ __device__ double recheck64(const TileArgs &a, int ipos, int jpos)
 
 // Squared distance t + lo (double-float, scaled units) of one pair from its
 // accumulators and split norms.
+// In units of the accumulators the distance is nu_i + nu_j - H - L; rc = -g
+// scales it back (exactly: g is a power of two).
 template <bool EXACT>
 __device__ __forceinline__ void assemble(float H, float L, float an_hi, float an_lo, float bn_hi, float bn_lo,
                                          float rc, float &t, float &lo, float &s)
 {
-  s = an_hi + bn_hi;                          // exact on the grid q
-  const float pL = L * rc, pH = H * rc;       // exact (rc is a power of 2)
+  s = an_hi + bn_hi;                          // exact on the grid q / g
+  float tt, ee;
   if constexpr (EXACT) {
-    const float t1 = s + pH;                  // exact: both on the grid q, |t1| < 2^24 q
-    t = t1 + pL;
-    lo = (an_lo + bn_lo) + (pL - (t - t1));   // Fast2Sum
+    const float t1 = s - H;                   // exact: H is an integer and q / g divides 1
+    tt = t1 - L;
+    ee = (t1 - tt) - L;                       // Fast2Sum
   } else {
-    const float u1 = s + pL;
-    const float e1 = pL - (u1 - s);           // Fast2Sum: |s| >= |pL|
-    t = u1 + pH;
-    const float e2 = pH - (t - u1);           // Fast2Sum: |u1| >= |pH|
-    lo = ((an_lo + bn_lo) + e1) + e2;
+    const float u1 = s - L;
+    const float e1 = (s - u1) - L;            // Fast2Sum: |s| >= |L|
+    tt = u1 - H;
+    const float e2 = (u1 - tt) - H;           // Fast2Sum: |u1| >= |H|
+    ee = e1 + e2;
+  }
+  t = tt * -rc;
+  lo = ((an_lo + bn_lo) + ee) * -rc;
+  s *= -rc;
+}
+
+// NC columns of one row, Gaussian with the low norm parts folded into the
+// source weights and the row factor: kv = 2^-(g tt) (1 - ln2 g ee).
+template <int NC>
+__device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
+                                                const PtMeta *__restrict__ bm, float an_hi, float rc,
+                                                float (&acc)[4])
+{
+  const float cg = 0.69314718f * rc;          // -ln2 g
+#pragma unroll
+  for (int j = 0; j < NC; j++) {
+    const float4 m0 = *(const float4 *)&bm[j];   // nu_hi, 0, w', h
+    const float w = m0.z;
+    const float H = __uint_as_float(h[j]), L = __uint_as_float(l[j]);
+    const float t1 = (an_hi + m0.x) - H;      // exact
+    const float tt = t1 - L;
+    const float ee = (t1 - tt) - L;
+    const float e = ex2_approx(tt * rc);      // 2^-(g tt)
+    const float kv = fmaf(e, cg * ee, e);
+    acc[j & 3] = fmaf(kv, w, acc[j & 3]);
   }
 }
 
-// 32 columns of one row, distance kernels.  Returns the flagged columns.
-template <int KT, bool EXACT, bool FLAGS>
-__device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[32], const uint32_t (&l)[32],
+// NC columns of one row, distance kernels.  Returns the flagged columns.
+template <int KT, bool EXACT, bool FLAGS, int NC>
+__device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                               const PtMeta *__restrict__ bm, const PtMeta &am, float rc,
                                               const Params *P, const KParams &kp, float (&acc)[4])
 {
@@ -452,7 +499,7 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[32], const uin
   float t_flag = 0.f, rho = 0.f;
   if constexpr (FLAGS) { t_flag = P->t_flag; rho = P->rho; }
 #pragma unroll
-  for (int j = 0; j < 32; j++) {
+  for (int j = 0; j < NC; j++) {
     const float4 m0 = *(const float4 *)&bm[j];   // n_hi, n_lo, w, h
     float t, lo, s;
     assemble<EXACT>(__uint_as_float(h[j]), __uint_as_float(l[j]), am.n_hi, am.n_lo, m0.x, m0.y, rc, t, lo, s);
@@ -468,14 +515,14 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[32], const uin
   return flags;
 }
 
-// 32 columns of one row, inner-product kernels (polynomial, tanh).
-template <int KT>
-__device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[32], const uint32_t (&l)[32],
+// NC columns of one row, inner-product kernels (polynomial, tanh).
+template <int KT, int NC>
+__device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                              const PtMeta *__restrict__ bm, int valid, float rc,
                                              const KParams &kp, float (&acc)[4])
 {
 #pragma unroll
-  for (int j = 0; j < 32; j++) {
+  for (int j = 0; j < NC; j++) {
     const float w = bm[j].w;
     const float cc = fmaf(__uint_as_float(l[j]), rc, __uint_as_float(h[j]) * rc) * -0.5f;  // x.y
     const float kv = kval32<KT>(0.f, 0.f, cc, 0.f, 0.f, kp);
@@ -483,13 +530,13 @@ __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[32], const uint
   }
 }
 
-// Test hook: raw accumulators and epilogue values of 32 columns.
-template <int KT>
-__device__ void dump_chunk(float *dump, int row, int ch, const uint32_t (&h)[32], const uint32_t (&l)[32],
+// Test hook: raw accumulators and epilogue values of NC columns from c0.
+template <int KT, int NC>
+__device__ void dump_chunk(float *dump, int row, int c0, const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                            const PtMeta *bm, const PtMeta &am, float rc, const KParams &kp)
 {
-  for (int j = 0; j < 32; j++) {
-    const int c = ch * 32 + j;
+  for (int j = 0; j < NC; j++) {
+    const int c = c0 + j;
     float *dp = dump + ((size_t)row * BN + c) * 5;
     const float H = __uint_as_float(h[j]), L = __uint_as_float(l[j]);
     dp[0] = H; dp[1] = L;
@@ -513,10 +560,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
   uint8_t *sm = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int kpad = a.kpad;
   const size_t a_bytes = tile_bytes(BM, kpad), b_bytes = tile_bytes(BN, kpad);
-  const size_t a_stride = (a_bytes + 1023) & ~(size_t)1023, b_stride = (b_bytes + 1023) & ~(size_t)1023;
+  const size_t bop_bytes = NBLK * blk_bytes(BN, kpad);          // source operands
+  const size_t bmeta_bytes = (size_t)BN * sizeof(PtMeta);       // source metadata
+  const size_t a_stride = (a_bytes + 1023) & ~(size_t)1023, b_stride = (bop_bytes + 1023) & ~(size_t)1023;
   uint8_t *sA = sm;
   uint8_t *sB = sm + a_stride;
-  SplitSmem *S = (SplitSmem *)(sB + NSTAGE * b_stride);
+  uint8_t *sBm = sB + NSTAGE * b_stride;                         // NMETA x bmeta_bytes
+  SplitSmem *S = (SplitSmem *)(sBm + NMETA * bmeta_bytes);
   volatile int *abort = &S->abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -525,7 +575,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
   if (threadIdx.x == 0) {
     mbar_init(&S->a_full, 1);
     mbar_init(&S->a_empty, 1 + EPI_WARPS);
-    for (int s = 0; s < NSTAGE; s++) { mbar_init(&S->b_full[s], 1); mbar_init(&S->b_empty[s], 1 + EPI_WARPS); }
+    for (int s = 0; s < NSTAGE; s++) { mbar_init(&S->b_full[s], 1); mbar_init(&S->b_empty[s], 1); }
+    for (int s = 0; s < NMETA; s++) { mbar_init(&S->m_full[s], 1); mbar_init(&S->m_empty[s], EPI_WARPS); }
     for (int b = 0; b < 2; b++) { mbar_init(&S->t_full[b], 1); mbar_init(&S->t_empty[b], EPI_WARPS); }
     mbar_init(&S->drain, 1);
     S->abort = 0;
@@ -543,8 +594,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     if (lane == 0) {
       int g = 0;
       int a_issued = -1;                 // item index of the last target-tile copy
-      int b_last[NSTAGE];                // use count of the last copy per stage
+      int b_last[NSTAGE], m_last[NMETA];  // use count of the last copy per stage / meta slot
       for (int s = 0; s < NSTAGE; s++) b_last[s] = -1;
+      for (int s = 0; s < NMETA; s++) m_last[s] = -1;
       for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
         const int ti = item % a.ntm, sc = item / a.ntm;
         if (it > 0 && !mbar_wait(&S->a_empty, (it - 1) & 1, abort, WAIT_LIMIT)) break;
@@ -555,9 +607,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         for (int tj = t0; tj < t1; tj++, g++) {
           const int st = g % NSTAGE, u = g / NSTAGE;
           if (u > 0 && !mbar_wait(&S->b_empty[st], (u - 1) & 1, abort, WAIT_LIMIT)) break;
-          mbar_arrive_expect_tx(&S->b_full[st], (uint32_t)b_bytes);
-          bulk_g2s(sB + st * b_stride, a.imgB + (size_t)tj * b_bytes, (uint32_t)b_bytes, &S->b_full[st]);
+          mbar_arrive_expect_tx(&S->b_full[st], (uint32_t)bop_bytes);
+          bulk_g2s(sB + st * b_stride, a.imgB + (size_t)tj * b_bytes, (uint32_t)bop_bytes, &S->b_full[st]);
           b_last[st] = u;
+          const int ms = g % NMETA, mu = g / NMETA;
+          if (mu > 0 && !mbar_wait(&S->m_empty[ms], (mu - 1) & 1, abort, WAIT_LIMIT)) break;
+          mbar_arrive_expect_tx(&S->m_full[ms], (uint32_t)bmeta_bytes);
+          bulk_g2s(sBm + ms * bmeta_bytes, a.imgB + (size_t)tj * b_bytes + bop_bytes, (uint32_t)bmeta_bytes,
+                   &S->m_full[ms]);
+          m_last[ms] = mu;
         }
       }
       // On an abort, let the copies already issued land before the CTA exits
@@ -567,6 +625,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         if (a_issued >= 0) mbar_wait(&S->a_full, a_issued & 1, nev, 1LL << 28);
         for (int s = 0; s < NSTAGE; s++)
           if (b_last[s] >= 0) mbar_wait(&S->b_full[s], b_last[s] & 1, nev, 1LL << 28);
+        for (int s = 0; s < NMETA; s++)
+          if (m_last[s] >= 0) mbar_wait(&S->m_full[s], m_last[s] & 1, nev, 1LL << 28);
       }
     }
   } else if (warp == 1) {
@@ -610,15 +670,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     }
   } else {
     // ---------------- epilogue (warps 2 .. 2+EPI_WARPS-1) ----------------
-    // Two groups of four warps; group g takes columns [64g, 64g+64) of every
-    // tile, each warp the 32 TMEM lanes (= target rows) of its sub-partition.
+    // EPI_GROUPS groups of four warps; group g takes columns [32g, 32g+32) of
+    // every tile, each warp the 32 TMEM lanes (= target rows) of its
+    // sub-partition, in two 16-column TMEM loads.
     const int ew = warp - 2;
     const int grp = ew >> 2;
     const int qd = warp & 3;
     const int row = qd * 32 + lane;
     const Params *P = a.P;
     const float rc = P->rc;
-    const bool flags_on = P->any_flag != 0, exact = P->exact_t1 != 0;
+    const bool flags_on = P->any_flag != 0, exact = P->exact_t1 != 0, gfast = P->gfast != 0;
     int g = 0, tc = 0;
     for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
       const int ti = item % a.ntm, sc = item / a.ntm;
@@ -630,54 +691,64 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       const int t0 = sc * a.chunk_tiles, t1 = min(a.ntn, t0 + a.chunk_tiles);
       bool ok = true;
       for (int tj = t0; tj < t1; tj++, g++, tc++) {
-        const int st = g % NSTAGE, buf = tc & 1;
+        const int ms = g % NMETA, buf = tc & 1;
         if (!mbar_wait(&S->t_full[buf], (tc >> 1) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
-        if (!mbar_wait(&S->b_full[st], (g / NSTAGE) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
+        if (!mbar_wait(&S->m_full[ms], (g / NMETA) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
         tc_fence_after();
-        const PtMeta *bm = (const PtMeta *)(sB + st * b_stride + NBLK * blk_bytes(BN, kpad));
+        const PtMeta *bm = (const PtMeta *)(sBm + ms * bmeta_bytes);
         const int ncols = min(BN, a.n - tj * BN);
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
         const uint32_t tH = tmem + ((uint32_t)(qd * 32) << 16) + buf * 256;
 #pragma unroll 1
-        for (int ch = 2 * grp; ch < 2 * grp + 2; ch++) {
-          uint32_t h[32], l[32];
-          tmem_ld32(tH + ch * 32, h);
-          tmem_ld32(tH + 128 + ch * 32, l);
+        for (int half = 0; half < 2; half++) {
+          const int c0 = grp * 32 + half * 16;
+          uint32_t h[16], l[16];
+          tmem_ld16(tH + c0, h);
+          tmem_ld16(tH + 128 + c0, l);
           tmem_ld_wait();
-          uint32_t flags = 0;
-          if constexpr (kt_uses_norms(KT)) {
-            if (exact) {
-              if (flags_on) flags = epi_chunk<KT, true, true>(h, l, bm + ch * 32, am, rc, P, a.kp, acc);
-              else epi_chunk<KT, true, false>(h, l, bm + ch * 32, am, rc, P, a.kp, acc);
-            } else {
-              if (flags_on) flags = epi_chunk<KT, false, true>(h, l, bm + ch * 32, am, rc, P, a.kp, acc);
-              else epi_chunk<KT, false, false>(h, l, bm + ch * 32, am, rc, P, a.kp, acc);
+          if constexpr (KT == KS_GAUSSIAN) {
+            if (gfast) {
+              epi_chunk_gfast<16>(h, l, bm + c0, am.n_hi, rc, acc);
+              if (a.dump && blockIdx.x == 0 && tc == 0) dump_chunk<KT, 16>(a.dump, row, c0, h, l, bm + c0, am, rc, a.kp);
+              continue;
             }
-            // FP64 rechecks of the flagged pairs of this 32-column chunk
+          }
+          if constexpr (kt_uses_norms(KT)) {
+            uint32_t flags = 0;
+            if (exact) {
+              if (flags_on) flags = epi_chunk<KT, true, true, 16>(h, l, bm + c0, am, rc, P, a.kp, acc);
+              else epi_chunk<KT, true, false, 16>(h, l, bm + c0, am, rc, P, a.kp, acc);
+            } else {
+              if (flags_on) flags = epi_chunk<KT, false, true, 16>(h, l, bm + c0, am, rc, P, a.kp, acc);
+              else epi_chunk<KT, false, false, 16>(h, l, bm + c0, am, rc, P, a.kp, acc);
+            }
+            // FP64 rechecks of the flagged pairs of these 16 columns
             while (flags) {
               const int j = __ffs(flags) - 1;
               flags &= flags - 1;
-              const int c = ch * 32 + j;
+              const int c = c0 + j;
               if (c < ncols && am.pos >= 0) racc += recheck64<KT>(a, am.pos, bm[c].pos);
             }
           } else {
-            epi_chunk_ip<KT>(h, l, bm + ch * 32, ncols - ch * 32, rc, a.kp, acc);
+            epi_chunk_ip<KT, 16>(h, l, bm + c0, ncols - c0, rc, a.kp, acc);
           }
-          if (a.dump && blockIdx.x == 0 && tc == 0) dump_chunk<KT>(a.dump, row, ch, h, l, bm + ch * 32, am, rc, a.kp);
+          if (a.dump && blockIdx.x == 0 && tc == 0) dump_chunk<KT, 16>(a.dump, row, c0, h, l, bm + c0, am, rc, a.kp);
         }
         racc += ((double)acc[0] + (double)acc[1]) + ((double)acc[2] + (double)acc[3]);
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) { mbar_arrive(&S->t_empty[buf]); mbar_arrive(&S->b_empty[st]); }
+        if (lane == 0) { mbar_arrive(&S->t_empty[buf]); mbar_arrive(&S->m_empty[ms]); }
       }
       if (!ok) break;
-      // combine the two column groups' row sums (double-buffered by item parity)
-      double *xs = S->rsum[it & 1];
-      if (grp == 1) xs[row] = racc;
+      // combine the groups' row sums in group order (double-buffered by item parity)
+      double (*xs)[BM] = S->rsum[it & 1];
+      if (grp > 0) xs[grp - 1][row] = racc;
       asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");
       if (grp == 0) {
+        for (int q = 0; q < EPI_GROUPS - 1; q++) racc += xs[q][row];
         const int grow = ti * BM + row;
-        if (grow < a.m) a.partial[(size_t)sc * a.ldp + grow] = racc + xs[row];
+        if (KT == KS_GAUSSIAN && gfast) racc *= (double)am.h;   // the row's low-norm factor
+        if (grow < a.m) a.partial[(size_t)sc * a.ldp + grow] = racc;
       }
     }
   }
@@ -730,11 +801,9 @@ cudaError_t launch_tiles(const TileArgs &a, int grid, size_t smem, cudaStream_t 
 
 size_t smem_bytes(int kpad)
 {
-  const size_t a = (tile_bytes(BM, kpad) + 1023) & ~(size_t)1023;
-  const size_t b = (tile_bytes(BN, kpad) + 1023) & ~(size_t)1023;
-  // + 32 KiB of tail slack: no descriptor of this kernel can make the tensor
-  // cores read past the allocation, whatever the core-matrix strides
-  return 1024 /* alignment slack */ + a + NSTAGE * b + sizeof(SplitSmem) + 64 + 32768;
+  const size_t a = (tile_bytes(BM, kpad) + 1023) & ~(size_t)1023;         // target image (resident)
+  const size_t b = (NBLK * blk_bytes(BN, kpad) + 1023) & ~(size_t)1023;   // source operand stage
+  return 1024 /* alignment slack */ + a + NSTAGE * b + NMETA * (size_t)BN * sizeof(PtMeta) + sizeof(SplitSmem) + 64;
 }
 
 }  // namespace split
