@@ -92,6 +92,47 @@ __host__ __device__ inline size_t tile_bytes(int rows, int kpad)
   return NBLK * blk_bytes(rows, kpad) + (size_t)rows * sizeof(PtMeta);
 }
 
+// k is processed in chunks of KCH (the whole padded k when it is smaller);
+// beyond KPAD_MAX the target tile no longer stays resident and both operands
+// stream through the stages chunk by chunk.
+constexpr int KCH = 64;
+__host__ __device__ inline int kchunk(int kpad) { return kpad < KCH ? kpad : KCH; }
+
+// Byte offset, inside a 128-row tile image, of the 16-byte row segment
+// (slice b, k-group kg, row r): chunk-major, then slice, then the no-swizzle
+// K-major core-matrix layout of the chunk (k-group, row, 8 elements).
+__host__ __device__ inline size_t img_off(int b, int kg, int r, int kpad)
+{
+  const int kc = kchunk(kpad), gpc = kc / 8;
+  const int c = kg / gpc, kgc = kg - c * gpc;
+  return (size_t)c * NBLK * BM * kc * 2 + (size_t)b * BM * kc * 2 + (size_t)kgc * BM * 16 + (size_t)r * 16;
+}
+
+// Shared-memory plan of split_tiles for a padded k.
+struct SmemLayout {
+  bool resident;       // the target tile stays in shared memory for the item
+  int kc, nch;         // k-chunk and number of chunks
+  int nstage;          // operand stages
+  size_t chunk_op;     // bytes of one operand's chunk (3 slices x 128 rows x kc)
+  size_t chunk_al;     // chunk_op rounded up to 1 KiB
+  size_t stage_bytes;  // one stage: the source chunk, or both operands' chunks
+  size_t a_region;     // target image (resident) or target metadata
+};
+__host__ __device__ inline SmemLayout smem_layout(int kpad)
+{
+  SmemLayout L;
+  L.kc = kchunk(kpad);
+  L.nch = kpad / L.kc;
+  L.resident = (L.nch == 1);
+  L.chunk_op = (size_t)NBLK * BM * L.kc * 2;
+  L.chunk_al = (L.chunk_op + 1023) & ~(size_t)1023;
+  L.nstage = L.resident ? NSTAGE : 2;
+  L.stage_bytes = L.resident ? L.chunk_al : 2 * L.chunk_al;
+  L.a_region = L.resident ? ((tile_bytes(BM, kpad) + 1023) & ~(size_t)1023)
+                          : (((size_t)BM * sizeof(PtMeta) + 1023) & ~(size_t)1023);
+  return L;
+}
+
 // ---------------------------------------------------------------------------
 // Ordered 64-bit keys of doubles, so that integer min/max is the double's.
 __device__ __forceinline__ long long dkey(double v)
@@ -254,11 +295,11 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
       s2[e] = h2;
       s3[e] = h3;
     }
-    const size_t off = (size_t)kg * BM * 16 + (size_t)r * 16;
-    *(uint4 *)(base + 0 * bb + off) = *(const uint4 *)s1;
-    *(uint4 *)(base + 1 * bb + off) = *(const uint4 *)s2;
-    *(uint4 *)(base + 2 * bb + off) = *(const uint4 *)s3;
+    *(uint4 *)(base + img_off(0, kg, r, kpad)) = *(const uint4 *)s1;
+    *(uint4 *)(base + img_off(1, kg, r, kpad)) = *(const uint4 *)s2;
+    *(uint4 *)(base + img_off(2, kg, r, kpad)) = *(const uint4 *)s3;
   }
+  (void)bb;
   // The norm in units of the accumulators: nu = |x''|^2 / g with
   // g = 2 sigma^2 2^-14, so that d2 = g (nu_i + nu_j - H - L).  nu is split on
   // the grid q / g (a power of two): its high parts and H add exactly.
@@ -559,14 +600,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *sm = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int kpad = a.kpad;
+  const SmemLayout L = smem_layout(kpad);
+  const bool resident = L.resident;
   const size_t a_bytes = tile_bytes(BM, kpad), b_bytes = tile_bytes(BN, kpad);
-  const size_t bop_bytes = NBLK * blk_bytes(BN, kpad);          // source operands
-  const size_t bmeta_bytes = (size_t)BN * sizeof(PtMeta);       // source metadata
-  const size_t a_stride = (a_bytes + 1023) & ~(size_t)1023, b_stride = (bop_bytes + 1023) & ~(size_t)1023;
-  uint8_t *sA = sm;
-  uint8_t *sB = sm + a_stride;
-  uint8_t *sBm = sB + NSTAGE * b_stride;                         // NMETA x bmeta_bytes
-  SplitSmem *S = (SplitSmem *)(sBm + NMETA * bmeta_bytes);
+  const size_t a_op = NBLK * blk_bytes(BM, kpad);     // operand part of a tile image
+  const size_t meta_bytes = (size_t)BM * sizeof(PtMeta);
+  uint8_t *sA = sm;                                   // target image (resident) or target meta
+  uint8_t *sAmeta = resident ? sA + a_op : sA;
+  uint8_t *sStage = sm + L.a_region;
+  uint8_t *sBm = sStage + L.nstage * L.stage_bytes;   // NMETA source metadata slots
+  SplitSmem *S = (SplitSmem *)(sBm + NMETA * meta_bytes);
   volatile int *abort = &S->abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -591,30 +634,50 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
 
   if (warp == 0) {
     // ---------------- producer ----------------
+    // Resident (k <= KPAD_MAX): the target tile image once per item, the source
+    // operands once per tile.  Streaming: the target metadata once per item,
+    // then per tile and k-chunk one stage holding both operands' chunk.
     if (lane == 0) {
-      int g = 0;
-      int a_issued = -1;                 // item index of the last target-tile copy
+      int g = 0, tt = 0;
+      int a_issued = -1;                  // item index of the last target copy
       int b_last[NSTAGE], m_last[NMETA];  // use count of the last copy per stage / meta slot
       for (int s = 0; s < NSTAGE; s++) b_last[s] = -1;
       for (int s = 0; s < NMETA; s++) m_last[s] = -1;
-      for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
+      bool stop = false;
+      for (int it = 0, item = blockIdx.x; item < items && !*abort && !stop; it++, item += gridDim.x) {
         const int ti = item % a.ntm, sc = item / a.ntm;
         if (it > 0 && !mbar_wait(&S->a_empty, (it - 1) & 1, abort, WAIT_LIMIT)) break;
-        mbar_arrive_expect_tx(&S->a_full, (uint32_t)a_bytes);
-        bulk_g2s(sA, a.imgA + (size_t)ti * a_bytes, (uint32_t)a_bytes, &S->a_full);
+        const uint8_t *imgA = a.imgA + (size_t)ti * a_bytes;
+        if (resident) {
+          mbar_arrive_expect_tx(&S->a_full, (uint32_t)a_bytes);
+          bulk_g2s(sA, imgA, (uint32_t)a_bytes, &S->a_full);
+        } else {
+          mbar_arrive_expect_tx(&S->a_full, (uint32_t)meta_bytes);
+          bulk_g2s(sAmeta, imgA + a_op, (uint32_t)meta_bytes, &S->a_full);
+        }
         a_issued = it;
         const int t0 = sc * a.chunk_tiles, t1 = min(a.ntn, t0 + a.chunk_tiles);
-        for (int tj = t0; tj < t1; tj++, g++) {
-          const int st = g % NSTAGE, u = g / NSTAGE;
-          if (u > 0 && !mbar_wait(&S->b_empty[st], (u - 1) & 1, abort, WAIT_LIMIT)) break;
-          mbar_arrive_expect_tx(&S->b_full[st], (uint32_t)bop_bytes);
-          bulk_g2s(sB + st * b_stride, a.imgB + (size_t)tj * b_bytes, (uint32_t)bop_bytes, &S->b_full[st]);
-          b_last[st] = u;
-          const int ms = g % NMETA, mu = g / NMETA;
+        for (int tj = t0; tj < t1 && !stop; tj++, tt++) {
+          const uint8_t *imgB = a.imgB + (size_t)tj * b_bytes;
+          for (int c = 0; c < L.nch; c++, g++) {
+            const int st = g % L.nstage, u = g / L.nstage;
+            if (u > 0 && !mbar_wait(&S->b_empty[st], (u - 1) & 1, abort, WAIT_LIMIT)) { stop = true; break; }
+            uint8_t *dst = sStage + st * L.stage_bytes;
+            if (resident) {
+              mbar_arrive_expect_tx(&S->b_full[st], (uint32_t)L.chunk_op);
+              bulk_g2s(dst, imgB, (uint32_t)L.chunk_op, &S->b_full[st]);
+            } else {
+              mbar_arrive_expect_tx(&S->b_full[st], (uint32_t)(2 * L.chunk_op));
+              bulk_g2s(dst, imgA + (size_t)c * L.chunk_op, (uint32_t)L.chunk_op, &S->b_full[st]);
+              bulk_g2s(dst + L.chunk_al, imgB + (size_t)c * L.chunk_op, (uint32_t)L.chunk_op, &S->b_full[st]);
+            }
+            b_last[st] = u;
+          }
+          if (stop) break;
+          const int ms = tt % NMETA, mu = tt / NMETA;
           if (mu > 0 && !mbar_wait(&S->m_empty[ms], (mu - 1) & 1, abort, WAIT_LIMIT)) break;
-          mbar_arrive_expect_tx(&S->m_full[ms], (uint32_t)bmeta_bytes);
-          bulk_g2s(sBm + ms * bmeta_bytes, a.imgB + (size_t)tj * b_bytes + bop_bytes, (uint32_t)bmeta_bytes,
-                   &S->m_full[ms]);
+          mbar_arrive_expect_tx(&S->m_full[ms], (uint32_t)meta_bytes);
+          bulk_g2s(sBm + ms * meta_bytes, imgB + a_op, (uint32_t)meta_bytes, &S->m_full[ms]);
           m_last[ms] = mu;
         }
       }
@@ -633,34 +696,39 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t idesc = idesc_f16_f32(BM, BN);
-      const uint32_t lbo_a = BM * 16, lbo_b = BN * 16, sbo = 128;
-      const uint32_t a0 = smem_addr(sA);
-      const size_t ab = blk_bytes(BM, kpad), bbk = blk_bytes(BN, kpad);
+      const uint32_t lbo = BM * 16, sbo = 128;        // BM == BN
+      const uint32_t blk = (uint32_t)BM * L.kc * 2;   // one slice block of one chunk
       int g = 0, tc = 0;
-      for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
+      bool stop = false;
+      for (int it = 0, item = blockIdx.x; item < items && !*abort && !stop; it++, item += gridDim.x) {
         const int sc = item / a.ntm;
         if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
         const int t0 = sc * a.chunk_tiles, t1 = min(a.ntn, t0 + a.chunk_tiles);
-        for (int tj = t0; tj < t1; tj++, g++, tc++) {
-          const int st = g % NSTAGE, buf = tc & 1;
-          if (!mbar_wait(&S->b_full[st], (g / NSTAGE) & 1, abort, WAIT_LIMIT)) break;
-          if (tc >= 2 && !mbar_wait(&S->t_empty[buf], ((tc >> 1) - 1) & 1, abort, WAIT_LIMIT)) break;
-          tc_fence_after();
-          const uint32_t b0 = smem_addr(sB + st * b_stride);
+        for (int tj = t0; tj < t1 && !stop; tj++, tc++) {
+          const int buf = tc & 1;
+          if (tc >= 2 && !mbar_wait(&S->t_empty[buf], ((tc >> 1) - 1) & 1, abort, WAIT_LIMIT)) { stop = true; break; }
           const uint32_t dH = tmem + buf * 256, dL = tmem + buf * 256 + 128;
-          for (int s = 0; s < kpad / 16; s++) {
-            const uint32_t ko = s * 2 * 16 * 128;  // two k-groups per step: 2 * rows * 16 bytes
-            auto da = [&](int blk) { return desc_noswizzle(a0 + blk * ab + (uint32_t)s * 2 * lbo_a, lbo_a, sbo); };
-            auto db = [&](int blk) { return desc_noswizzle(b0 + blk * bbk + (uint32_t)s * 2 * lbo_b, lbo_b, sbo); };
-            (void)ko;
-            umma_f16(dH, da(0), db(0), idesc, s > 0);
-            umma_f16(dL, da(0), db(1), idesc, s > 0);
-            umma_f16(dL, da(1), db(0), idesc, 1);
-            umma_f16(dL, da(1), db(1), idesc, 1);
-            umma_f16(dL, da(0), db(2), idesc, 1);
-            umma_f16(dL, da(2), db(0), idesc, 1);
+          for (int c = 0; c < L.nch; c++, g++) {
+            const int st = g % L.nstage;
+            if (!mbar_wait(&S->b_full[st], (g / L.nstage) & 1, abort, WAIT_LIMIT)) { stop = true; break; }
+            tc_fence_after();
+            const uint32_t sbase = smem_addr(sStage + st * L.stage_bytes);
+            const uint32_t a0 = resident ? smem_addr(sA) : sbase;
+            const uint32_t b0 = resident ? sbase : sbase + (uint32_t)L.chunk_al;
+            for (int s = 0; s < L.kc / 16; s++) {
+              auto da = [&](int b) { return desc_noswizzle(a0 + b * blk + (uint32_t)s * 2 * lbo, lbo, sbo); };
+              auto db = [&](int b) { return desc_noswizzle(b0 + b * blk + (uint32_t)s * 2 * lbo, lbo, sbo); };
+              const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
+              umma_f16(dH, da(0), db(0), idesc, acc);
+              umma_f16(dL, da(0), db(1), idesc, acc);
+              umma_f16(dL, da(1), db(0), idesc, 1);
+              umma_f16(dL, da(1), db(1), idesc, 1);
+              umma_f16(dL, da(0), db(2), idesc, 1);
+              umma_f16(dL, da(2), db(0), idesc, 1);
+            }
+            umma_commit(&S->b_empty[st]);
           }
-          umma_commit(&S->b_empty[st]);
+          if (stop) break;
           umma_commit(&S->t_full[buf]);
         }
         umma_commit(&S->a_empty);
@@ -684,7 +752,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
       const int ti = item % a.ntm, sc = item / a.ntm;
       if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
-      const PtMeta am = ((const PtMeta *)(sA + NBLK * blk_bytes(BM, kpad)))[row];
+      const PtMeta am = ((const PtMeta *)sAmeta)[row];
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->a_empty);
       double racc = 0.0;
@@ -695,7 +763,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         if (!mbar_wait(&S->t_full[buf], (tc >> 1) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
         if (!mbar_wait(&S->m_full[ms], (g / NMETA) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
         tc_fence_after();
-        const PtMeta *bm = (const PtMeta *)(sBm + ms * bmeta_bytes);
+        const PtMeta *bm = (const PtMeta *)(sBm + ms * meta_bytes);
         const int ncols = min(BN, a.n - tj * BN);
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
         const uint32_t tH = tmem + ((uint32_t)(qd * 32) << 16) + buf * 256;
@@ -801,9 +869,9 @@ cudaError_t launch_tiles(const TileArgs &a, int grid, size_t smem, cudaStream_t 
 
 size_t smem_bytes(int kpad)
 {
-  const size_t a = (tile_bytes(BM, kpad) + 1023) & ~(size_t)1023;         // target image (resident)
-  const size_t b = (NBLK * blk_bytes(BN, kpad) + 1023) & ~(size_t)1023;   // source operand stage
-  return 1024 /* alignment slack */ + a + NSTAGE * b + NMETA * (size_t)BN * sizeof(PtMeta) + sizeof(SplitSmem) + 64;
+  const SmemLayout L = smem_layout(kpad);
+  return 1024 /* alignment slack */ + L.a_region + L.nstage * L.stage_bytes + NMETA * (size_t)BN * sizeof(PtMeta) +
+         sizeof(SplitSmem) + 64;
 }
 
 }  // namespace split
@@ -821,8 +889,9 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
 {
   using namespace split;
   (void)XA2; (void)XB2; (void)nxa; (void)nxb;
-  const int kpad = (k + 15) / 16 * 16;
-  if (kpad > KPAD_MAX) return GSKS_ERR_TOO_LARGE;
+  // padded k: a multiple of the MMA k-step (16) up to one chunk, of the chunk beyond
+  const int kpad = k <= KCH ? (k + 15) / 16 * 16 : (k + KCH - 1) / KCH * KCH;
+  if (kpad > 1024) return GSKS_ERR_TOO_LARGE;   // the exact head accumulation needs k <= 1024
   const int ntm = (m + BM - 1) / BM, ntn = (n + BN - 1) / BN;
   const int sms = std::max(1, c->num_sms);
   int nsc = (int)std::min<long long>(ntn, std::max<long long>(1, (8LL * sms + ntm - 1) / ntm));

@@ -81,3 +81,50 @@ def test_split_var_bandwidth(gpu, oracle_mod):
     h = np.exp(rng.uniform(np.log(0.05), np.log(0.5), X.shape[0]))
     e = _run(gpu, oracle_mod, 3, {}, X, w, amap, bmap, umap, wmap, hi=1.0 / h)
     assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+@pytest.mark.parametrize("shape", [(3000, 128, 300, 400), (2000, 512, 200, 300), (1500, 1000, 150, 200),
+                                   (2500, 80, 260, 390)])
+def test_split_gaussian_streamed_k(gpu, oracle_mod, shape):
+    """k beyond the target-resident kernel: both operands stream in 64-wide k chunks."""
+    N, k, m, n = shape
+    e = _run(gpu, oracle_mod, 0, dict(scal=-12.0 / k), *_case(5, N, k, m, n))
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+def test_split_polynomial_dense_k1024(gpu, oracle_mod):
+    """The dense configuration's shape at a small size: N(0, 1/k) points, k = 1024, pwr 4."""
+    X, w, amap, bmap, umap, wmap = _case(6, 1200, 1024, 160, 170, dist="normal")
+    e = _run(gpu, oracle_mod, 1, dict(scal=1.0, cons=1.0, powe=4.0), X / np.sqrt(1024), w, amap, bmap, umap, wmap)
+    assert e["cond_max"] <= TOL, e
+
+
+def _mixture(seed, N, k, ncl=64, sigma=0.05, dup=0.01):
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-10, 10, (ncl, k))
+    lab = rng.integers(0, ncl, N)
+    X = centres[lab] + sigma * rng.standard_normal((N, k))
+    nd = int(dup * N)
+    src = rng.choice(N, nd, replace=False)
+    dst = rng.choice(N, nd, replace=False)
+    X[dst] = X[src]                       # exact duplicates
+    return X
+
+
+@pytest.mark.parametrize("k", [3, 8, 32, 128, 512])
+def test_split_mixture_with_duplicates(gpu, oracle_mod, k):
+    """The split-precision configuration's data at a reduced size: 64-component
+    Gaussian mixture (centres U[-10,10]^k, sigma 0.05) with 1% exact duplicates;
+    Gaussian h = 0.2 and polynomial pwr 2."""
+    N, m, n = 6000, 1500, 1500
+    X = _mixture(10 + k, N, k)
+    rng = np.random.default_rng(20 + k)
+    w = rng.standard_normal(N)
+    amap = rng.choice(N, m, replace=False).astype(np.int32)
+    bmap = rng.choice(N, n, replace=False).astype(np.int32)
+    umap = rng.permutation(N)[:m].astype(np.int32)
+    wmap = rng.permutation(N)[:n].astype(np.int32)
+    e = _run(gpu, oracle_mod, 0, dict(scal=-12.5), X, w, amap, bmap, umap, wmap)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, ("gaussian", e)
+    e = _run(gpu, oracle_mod, 1, dict(scal=1.0 / k, cons=1.0, powe=2.0), X, w, amap, bmap, umap, wmap)
+    assert e["cond_max"] <= TOL, ("polynomial", e)
