@@ -73,4 +73,14 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k,
                   const double *w, const int *wmap, const double *hi, const double *hj,
                   cudaStream_t s, bool stream_ordered_alloc);
 
+// Split-precision form of dgsks_list (gsks_split.cu): row sums of every
+// (task t, target position r, source chunk sc) into
+// partial[pbase[t] + sc * m_t + r], chunk sources per chunk (a multiple of
+// 128).  kps: ntask device-side descriptors; hoff_a / hoff_b: host offsets;
+// everything else device pointers.  Adds its launch count to *launches.
+int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
+                       const long long *pbase, int chunk, const double *XA, const int *a_idx, int nxa,
+                       const double *XB, const int *b_idx, int nxb, const double *w, const int *w_idx,
+                       double *partial, cudaStream_t s, int *launches);
+
 }  // namespace gsks

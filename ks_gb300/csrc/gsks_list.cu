@@ -9,6 +9,9 @@
 // kernel then adds, for each distinct u entry, the contributions of all list
 // positions that name it in ascending position order -- the same order on
 // every run, so the result is deterministic without floating-point atomics.
+// With the split-precision form selected, the same partial layout is filled
+// by the tensor-core kernel of gsks_split.cu (enqueue_split_list) and merged
+// by the same merge kernel.
 #include "gsks.h"
 #include "gsks_internal.cuh"
 #include "gsks_host.h"
@@ -150,7 +153,8 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
   ListBufs &L = *tl_list;
   const bool dev = is_device_pointer(XA);
   const int prec = effective_precision();
-  if (prec != GSKS_FP64) return set_status(GSKS_ERR_PRECISION, "dgsks_list");
+  if (prec != GSKS_FP64 && prec != GSKS_SPLIT_BF16X3) return set_status(GSKS_ERR_PRECISION, "dgsks_list");
+  const bool split = prec == GSKS_SPLIT_BF16X3;
 
   // ---- offsets and lists on the host ------------------------------------
   std::vector<int> hoff_a(ntask + 1), hoff_b(ntask + 1);
@@ -271,7 +275,7 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
   }
   if (!ok) return set_status(GSKS_ERR_ALLOC, "dgsks_list upload");
   int launches = 0;
-  if (any_norms) {
+  if (any_norms && !split) {   // the split form forms its own norms
     // caller-supplied norms are used as given; missing ones are computed on
     // the device (the list wrappers of frame/omp_dgsks_list.cpp:74-92)
     if (XA2) {
@@ -295,7 +299,7 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
       dXB2 = (const double *)L.XB2.p;
     }
   }
-  ok = upload(L.items, items.data(), items.size(), s) && upload(L.tasks, tasks.data(), tasks.size(), s) &&
+  ok = (split || upload(L.items, items.data(), items.size(), s)) && upload(L.tasks, tasks.data(), tasks.size(), s) &&
        upload(L.kps, kps.data(), kps.size(), s) && upload(L.ent_u, ent_u.data(), ent_u.size(), s) &&
        upload(L.own_off, own_off.data(), own_off.size(), s) &&
        upload(L.own_pos, own_pos.data(), own_pos.size(), s) &&
@@ -307,8 +311,16 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
   FusedArgs a{};
   a.k = k; a.XA = dXA; a.XA2 = dXA2; a.amap = da_idx; a.XB = dXB; a.XB2 = dXB2; a.bmap = db_idx;
   a.w = dw; a.wmap = dw_idx; a.nxa = nxa; a.nxb = nxb; a.err = (int *)c->err.p;
-  cudaMemsetAsync(L.counter.p, 0, sizeof(int), s);
-  if (!items.empty()) {
+  if (split) {
+    std::vector<KParams> kpt(ntask);
+    std::vector<long long> pb(ntask);
+    for (int t = 0; t < ntask; t++) { kpt[t] = kps[kernels ? t : 0]; pb[t] = tasks[t].pbase; }
+    const int st = enqueue_split_list(c, kpt.data(), ntask, k, hoff_a.data(), hoff_b.data(), pb.data(), LIST_CHUNK,
+                                      dXA, da_idx, nxa, dXB, db_idx, nxb, dw, dw_idx, (double *)L.partial.p, s,
+                                      &launches);
+    if (st) return set_status(st, "dgsks_list split");
+  } else if (!items.empty()) {
+    cudaMemsetAsync(L.counter.p, 0, sizeof(int), s);
     const int grid = std::max(1, std::min<int>((int)items.size(), c->num_sms * 2));
     list_fp64_kernel<<<grid, fp64cfg::NT, 0, s>>>(a, (const KParams *)L.kps.p, kernels ? 1 : 0,
                                                   (const ListItem *)L.items.p, (int)items.size(),

@@ -47,6 +47,8 @@
 #include <cuda_fp16.h>
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <vector>
 
 namespace gsks {
 namespace split {
@@ -70,7 +72,8 @@ struct PtMeta {          // 32 bytes per point, appended to each tile image
   float w;               // sources: w[wmap[j]]; targets: unused
   float h;               // var-bandwidth factor (targets: -0.5 log2e hi; sources: hj)
   int pos;               // position in amap / bmap, -1 for padding
-  int pad[3];
+  int pad[3];            // [0] sources, column 32g: bits of sum |w| over columns 32g..32g+31
+                         // [1] var-bandwidth: low part of h (float bits)
 };
 
 struct Params {          // per call, computed on the device
@@ -84,6 +87,30 @@ struct Params {          // per call, computed on the device
   int exact_t1;          // nu_i + nu_j - H is exact in FP32
   int gfast;             // Gaussian without flags: low norm parts folded into w / row factors
   float c0h, c0l;        // Laplace: scal^(1/m), m = -powe, as a double-float
+  double delta;          // absolute error bound of the assembled d2 (scaled units)
+};
+
+// Kernel selector of the batched (list) form: the epilogue dispatches on each
+// task's type; the Gaussian then takes its scale per task (coordinates unscaled).
+constexpr int KS_LIST = 99;
+constexpr int KS_GAUSS_UNSCALED = 100;
+
+// Epilogue parameters of one task (a single call uses one, built from Params).
+struct TaskParam {
+  KParams kp;
+  float t_flag, rho;     // flag pairs with t < t_flag or t < rho * (n_i + n_j)
+  float s2, s2l;         // Gaussian of the list form: scal * log2(e) = s2 + s2l
+  float c0h, c0l;        // Laplace: scal^(1/m), m = -powe
+  int any_flag;
+  int centred;           // distance kernels: coordinates taken relative to the centre
+};
+
+// One work item of the list form: a target tile and a range of source tiles of
+// one task; the rows' partial sums go to partial[out + row].
+struct SplitItem {
+  int a_tile, b0, b1, task;
+  long long out;
+  int rows, pad;
 };
 
 __host__ __device__ inline size_t blk_bytes(int rows, int kpad) { return (size_t)rows * kpad * 2; }
@@ -153,9 +180,19 @@ __global__ void bbox_init(int k, long long *bbox)
   }
 }
 
+// Map entry -> pool index; an entry outside [0, npool) (npool >= 0) raises
+// DEVERR_MAP_RANGE and reads point 0 instead.
+__device__ __forceinline__ int pool_index(const int *map, int pos, int npool, int *err)
+{
+  int p = map ? map[pos] : pos;
+  if (npool >= 0 && (p < 0 || p >= npool)) { atomicOr(err, DEVERR_MAP_RANGE); p = 0; }
+  return p;
+}
+
 // Per-dimension min / max over the gathered targets and sources.
 __global__ void bbox_kernel(int m, int n, int k, const double *__restrict__ XA, const int *__restrict__ amap,
-                            const double *__restrict__ XB, const int *__restrict__ bmap, long long *bbox)
+                            int nxa, const double *__restrict__ XB, const int *__restrict__ bmap, int nxb,
+                            int *err, long long *bbox)
 {
   extern __shared__ long long sb[];
   for (int p = threadIdx.x; p < k; p += blockDim.x) {
@@ -168,8 +205,8 @@ __global__ void bbox_kernel(int m, int n, int k, const double *__restrict__ XA, 
        e += (long long)blockDim.x * gridDim.x) {
     const int pt = (int)(e / k), p = (int)(e - (long long)pt * k);
     double v;
-    if (pt < m) v = XA[(size_t)(amap ? amap[pt] : pt) * k + p];
-    else v = XB[(size_t)(bmap ? bmap[pt - m] : pt - m) * k + p];
+    if (pt < m) v = XA[(size_t)pool_index(amap, pt, nxa, err) * k + p];
+    else v = XB[(size_t)pool_index(bmap, pt - m, nxb, err) * k + p];
     const long long key = dkey(v);
     atomicMin(&sb[p], key);
     atomicMax(&sb[k + p], key);
@@ -182,6 +219,9 @@ __global__ void bbox_kernel(int m, int n, int k, const double *__restrict__ XA, 
 }
 
 // Centre, scales and the flag thresholds from the bounding box (one block).
+// kt = KS_LIST: the list form, whose tasks mix centred (distance) and
+// uncentred (inner-product) kernels: the centre is the box's, the scale covers
+// the uncentred coordinates too, and the thresholds are set per task later.
 __global__ void params_kernel(int k, int kt, double scal, double powe, float tau, const long long *bbox,
                               double *centre, Params *P)
 {
@@ -191,7 +231,8 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
   for (int p = threadIdx.x; p < k; p += blockDim.x) {
     const double lo = dval(bbox[p]), hi = dval(bbox[k + p]);
     double c = 0.0, half;
-    if (dist) { c = 0.5 * (lo + hi); half = 0.5 * (hi - lo); }
+    if (kt == KS_LIST) { c = 0.5 * (lo + hi); half = fmax(fabs(lo), fabs(hi)); }
+    else if (dist) { c = 0.5 * (lo + hi); half = 0.5 * (hi - lo); }
     else half = fmax(fabs(lo), fabs(hi));
     centre[p] = c;
     sq += half * half;
@@ -224,12 +265,15 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     // |t + lo - d2| was 1.4e-7, and this expression gives 1.6e-7 there.)
     const double delta = 2.0 * (sigma * sigma * (double)k * 0x1p-31) +
                          2.0 * sigma * sqrt((double)k) * sqrt(nbound) * 0x1p-30 + 2.0 * q * 0x1p-23;
+    P->delta = delta;
     float t_flag = -1.0f, rho = 0.0f;
     if (kt == KS_GAUSSIAN) {
       // relative error of 2^-d2 is ln2 * delta; pairs with t >= 126 underflow anyway
       if (delta * 0.6931471805599453 > tau) t_flag = 126.0f;
     } else if (kt == KS_GAUSSIAN_VAR_BANDWIDTH) {
-      if (delta > tau) t_flag = 3.0e38f;      // bound not usable per pair: recheck all near pairs
+      // relative error of 2^(f d2) is ln2 f delta: pairs with a bandwidth
+      // product f above this cap (and no underflow) are rechecked
+      t_flag = (float)(tau / (0.6931471805599453 * delta));
     } else if (kt == KS_LAPLACE) {
       rho = 0x1p-10f;                         // coincident points and near-cancellation
       t_flag = (float)(fabs(powe) * delta / tau);
@@ -251,22 +295,67 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
   }
 }
 
+// Per-task epilogue parameters of the list form (coordinates unscaled, alpha = 1):
+// the flag thresholds of params_kernel with each task's own kernel.
+__global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, const Params *__restrict__ P,
+                                   float tau, TaskParam *__restrict__ out)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntask) return;
+  const KParams kp = kps[t];
+  const double delta = P->delta;
+  TaskParam T;
+  T.kp = kp;
+  T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.c0h = T.c0l = 0.0f;
+  T.centred = kt_uses_norms(kp.type) ? 1 : 0;
+  if (kp.type == KS_GAUSSIAN) {
+    const double s2 = kp.scal * 1.4426950408889634;
+    T.s2 = (float)s2;
+    T.s2l = (float)(s2 - (double)T.s2);
+    // relative error of 2^(s2 d2) is ln2 |s2| delta; beyond d2 = 126 / |s2| it underflows
+    if (0.6931471805599453 * fabs(s2) * delta > tau) T.t_flag = (float)(126.0 / fabs(s2));
+  } else if (kp.type == KS_GAUSSIAN_VAR_BANDWIDTH) {
+    T.t_flag = (float)(tau / (0.6931471805599453 * delta));   // cap on f, as params_kernel
+  } else if (kp.type == KS_LAPLACE) {
+    T.rho = 0x1p-10f;
+    T.t_flag = (float)(fabs(kp.powe) * delta / tau);
+    const double mm = -kp.powe, c0 = pow(kp.scal, 1.0 / mm);
+    T.c0h = (float)c0;
+    T.c0l = (float)(c0 - (double)T.c0h);
+    T.t_flag = fmaxf(T.t_flag, (float)(c0 * exp2(-120.0 / mm) * 1.001));
+  }
+  T.any_flag = (T.t_flag > 0.0f || T.rho > 0.0f) ? 1 : 0;
+  out[t] = T;
+}
+
 // Tile images: per tile, NBLK slice blocks in the no-swizzle K-major core-matrix
 // layout (element (r, p) at (p/8)*rows*16 + r*16 + (p%8)*2 bytes), then the
 // point metadata.  One thread per point.
+// List form (tiles != nullptr): tile t packs positions tiles[t].x ..
+// tiles[t].x + tiles[t].y - 1 of the CSR list `map`, for task tile_task[t].
 __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *__restrict__ X,
-                            const int *__restrict__ map, const double *__restrict__ w,
+                            const int *__restrict__ map, int npool, int *err, const double *__restrict__ w,
                             const int *__restrict__ wmap, const double *__restrict__ hvec, int kt,
                             const double *__restrict__ centre, const Params *__restrict__ P,
-                            uint8_t *__restrict__ img)
+                            uint8_t *__restrict__ img, const int2 *__restrict__ tiles,
+                            const int *__restrict__ tile_task, const TaskParam *__restrict__ tp)
 {
   const int tile = blockIdx.x, r = threadIdx.x;
-  const int pt = tile * BM + r;
-  const bool valid = pt < npts;
-  const int pidx = valid ? (map ? map[pt] : pt) : 0;
+  int pt = tile * BM + r;
+  bool valid = pt < npts;
+  bool centred = P->centred != 0;
+  if (tiles) {
+    const int2 tl = tiles[tile];
+    const TaskParam &T = tp[tile_task[tile]];
+    pt = tl.x + r;
+    valid = r < tl.y;
+    centred = T.centred != 0;
+    kt = T.kp.type;
+    hvec = side == 0 ? T.kp.hi : T.kp.hj;
+  }
+  const int pidx = valid ? pool_index(map, pt, npool, err) : 0;
   const double *x = X + (size_t)pidx * k;
   const double alpha = P->alpha, inv_sigma = P->inv_sigma;
-  const bool centred = P->centred != 0;
   uint8_t *base = img + (size_t)tile * tile_bytes(BM, kpad);
   const size_t bb = blk_bytes(BM, kpad);
   double nrm = 0.0;
@@ -322,12 +411,21 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
     if (side == 1) mt.w = valid ? (float)(w[wmap ? wmap[pt] : pt] * f) : 0.0f;
     else mt.h = (float)f;
   }
-  if (kt == KS_GAUSSIAN_VAR_BANDWIDTH && valid) {
-    const double hv = hvec[pidx];
-    mt.h = side == 0 ? (float)(-0.5 * 1.4426950408889634 * hv) : (float)hv;
-  }
   mt.pos = valid ? pt : -1;
   mt.pad[0] = mt.pad[1] = mt.pad[2] = 0;
+  if (kt == KS_GAUSSIAN_VAR_BANDWIDTH && valid) {
+    // the factor as a float pair h + pad[1]: an FP32 factor alone would put a
+    // relative error of 2^-24 on exponents of up to 126
+    const double hv = side == 0 ? -0.5 * 1.4426950408889634 * hvec[pidx] : hvec[pidx];
+    mt.h = (float)hv;
+    mt.pad[1] = __float_as_int((float)(hv - (double)mt.h));
+  }
+  // sources: sum of |w| over each group of 32 columns, kept with the group's
+  // first column (the underflow test of the exponential kernels)
+  float wa = fabsf(mt.w);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) wa += __shfl_xor_sync(0xffffffffu, wa, o);
+  if ((r & 31) == 0) mt.pad[0] = __float_as_int(wa);
   ((PtMeta *)(base + NBLK * bb))[r] = mt;
 }
 
@@ -338,6 +436,7 @@ struct TileArgs {
   const uint8_t *imgA, *imgB;
   const double *XA, *XB;            // pool coordinates (FP64) for the rechecks
   const int *amap, *bmap, *wmap;
+  int nxa, nxb;                     // pool sizes for the map range checks (-1: unchecked)
   const double *w;
   const double *hi, *hj;
   KParams kp;                       // FP64 descriptor for the rechecks
@@ -346,7 +445,36 @@ struct TileArgs {
   int ldp;
   int *err;
   float *dump;                      // test hook: H, L, t, lo, K of CTA 0's first tile
+  // list form: explicit work items and per-task parameters (nullptr otherwise)
+  const SplitItem *tab;
+  int ntab;
+  const TaskParam *tp;
+  const int *btile_cols;            // valid columns of each source tile
 };
+
+// Geometry of work item `item`: target tile, source-tile range, task, the
+// partial offset of row 0 and the number of valid rows.
+struct ItemGeo {
+  int ti, t0, t1, task, rows;
+  long long out;
+};
+__device__ __forceinline__ ItemGeo item_geo(const TileArgs &a, int item)
+{
+  ItemGeo g;
+  if (a.tab) {
+    const SplitItem it = a.tab[item];
+    g.ti = it.a_tile; g.t0 = it.b0; g.t1 = it.b1; g.task = it.task; g.out = it.out; g.rows = it.rows;
+  } else {
+    g.ti = item % a.ntm;
+    const int sc = item / a.ntm;
+    g.t0 = sc * a.chunk_tiles;
+    g.t1 = min(a.ntn, g.t0 + a.chunk_tiles);
+    g.task = 0;
+    g.out = (long long)sc * a.ldp + (long long)g.ti * BM;
+    g.rows = min(BM, a.m - g.ti * BM);
+  }
+  return g;
+}
 
 struct SplitSmem {
   uint64_t a_full, a_empty;
@@ -386,6 +514,17 @@ __device__ __forceinline__ void df_rcp(float &ah, float &al)
   ah = s;
 }
 
+// 2^((t + lo)(ph + pl)) for a double-float distance and a double-float factor
+// (ph + pl <= 0): the product's rounding and the low parts enter through the
+// first-order term.
+__device__ __forceinline__ float exp2_prod(float t, float lo, float ph, float pl)
+{
+  const float a = t * ph;
+  const float ae = fmaf(t, ph, -a) + fmaf(lo, ph, t * pl);
+  const float e = ex2_approx(a);
+  return fmaf(e, 0.69314718f * ae, e);
+}
+
 // FP32 kernel value from the double-float squared distance t + lo (scaled
 // units) or, for inner-product kernels, from c = x.y.
 template <int KT>
@@ -394,6 +533,12 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
   if constexpr (KT == KS_GAUSSIAN) {
     const float e = ex2_approx(-t);
     return fmaf(e, -0.69314718f * lo, e);
+  } else if constexpr (KT == KS_GAUSS_UNSCALED) {
+    // arg2 = s2 (t + lo), s2 = scal log2(e) passed in hrow
+    const float a = t * hrow;
+    const float ae = fmaf(t, hrow, -a) + lo * hrow;
+    const float e = ex2_approx(a);
+    return fmaf(e, 0.69314718f * ae, e);
   } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
     // arg2 = (t + lo) * hrow * hcol, hrow = -0.5 log2e hi
     const float f = hrow * hcol;
@@ -460,23 +605,25 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
 // FP64 recheck of one flagged pair from the pool coordinates (the distance
 // assembly of near-coincident pairs is kept in FP64).
 template <int KT>
-__device__ double recheck64(const TileArgs &a, int ipos, int jpos)
+__device__ double recheck64(const TileArgs &a, const KParams &kp, int ipos, int jpos)
 {
-  const int pa = a.amap ? a.amap[ipos] : ipos;
-  const int pb = a.bmap ? a.bmap[jpos] : jpos;
+  int pa = a.amap ? a.amap[ipos] : ipos;
+  int pb = a.bmap ? a.bmap[jpos] : jpos;
+  if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
+  if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
   const double *x = a.XA + (size_t)pa * a.k, *y = a.XB + (size_t)pb * a.k;
   double d2 = 0.0;
   for (int p = 0; p < a.k; p++) { const double d = x[p] - y[p]; d2 = fma(d, d, d2); }
   const double wv = a.w[a.wmap ? a.wmap[jpos] : jpos];
   double kv;
-  if constexpr (KT == KS_GAUSSIAN) kv = exp(d2 * a.kp.scal);
-  else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) kv = exp(((d2 * -0.5) * a.hi[pa]) * a.hj[pb]);
+  if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED) kv = exp(d2 * kp.scal);
+  else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) kv = exp(((d2 * -0.5) * kp.hi[pa]) * kp.hj[pb]);
   else if constexpr (KT == KS_LAPLACE) {
     if (d2 < 1e-15) d2 = 1.79e308;
-    kv = pow_class(d2, a.kp) * a.kp.scal;
+    kv = pow_class(d2, kp) * kp.scal;
   } else if constexpr (KT == KS_QUARTIC) {
     kv = d2 < 1.0 ? (15.0 / 16.0) * (1.0 - d2) * (1.0 - d2) : 0.0;
-  } else if constexpr (KT == KS_MULTIQUADRATIC) kv = d2 + a.kp.cons;
+  } else if constexpr (KT == KS_MULTIQUADRATIC) kv = d2 + kp.cons;
   else if constexpr (KT == KS_EPANECHNIKOV) kv = d2 < 1.0 ? 0.75 * (1.0 - d2) : 0.0;
   else kv = 0.0;
   return kv * wv;
@@ -534,21 +681,34 @@ __device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const u
 template <int KT, bool EXACT, bool FLAGS, int NC>
 __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                               const PtMeta *__restrict__ bm, const PtMeta &am, float rc,
-                                              const Params *P, const KParams &kp, float (&acc)[4])
+                                              const TaskParam &T, float (&acc)[4])
 {
+  const KParams &kp = T.kp;
   uint32_t flags = 0;
   float t_flag = 0.f, rho = 0.f;
-  if constexpr (FLAGS) { t_flag = P->t_flag; rho = P->rho; }
+  if constexpr (FLAGS) { t_flag = T.t_flag; rho = T.rho; }
 #pragma unroll
   for (int j = 0; j < NC; j++) {
     const float4 m0 = *(const float4 *)&bm[j];   // n_hi, n_lo, w, h
     float t, lo, s;
     assemble<EXACT>(__uint_as_float(h[j]), __uint_as_float(l[j]), am.n_hi, am.n_lo, m0.x, m0.y, rc, t, lo, s);
     float kv;
-    if constexpr (KT == KS_LAPLACE) kv = kval32<KT>(t, lo, 0.f, P->c0h, P->c0l, kp);
-    else kv = kval32<KT>(t, lo, 0.f, am.h, m0.w, kp);
+    if constexpr (KT == KS_LAPLACE) kv = kval32<KT>(t, lo, 0.f, T.c0h, T.c0l, kp);
+    else if constexpr (KT == KS_GAUSS_UNSCALED) kv = exp2_prod(t, lo, T.s2, T.s2l);
+    else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
+      // factor h_i h_j (negative) as a float pair
+      const float ph = am.h * m0.w;
+      const float pl = fmaf(am.h, m0.w, -ph) +
+                       fmaf(am.h, __int_as_float(bm[j].pad[1]), __int_as_float(am.pad[1]) * m0.w);
+      kv = exp2_prod(t, lo, ph, pl);
+    } else kv = kval32<KT>(t, lo, 0.f, am.h, m0.w, kp);
     if constexpr (FLAGS) {
-      if (t < t_flag || t < rho * s) { flags |= 1u << j; kv = 0.f; }
+      if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
+        const float f = -am.h * m0.w;             // 0.5 log2(e) h_i h_j
+        if (f > t_flag && t * f < 126.f) { flags |= 1u << j; kv = 0.f; }
+      } else {
+        if (t < t_flag || t < rho * s) { flags |= 1u << j; kv = 0.f; }
+      }
     }
     // padding columns carry w = 0 and finite distances
     acc[j & 3] = fmaf(kv, m0.z, acc[j & 3]);
@@ -594,6 +754,145 @@ __device__ void dump_chunk(float *dump, int row, int c0, const uint32_t (&h)[NC]
   }
 }
 
+__host__ __device__ constexpr bool kt_exponential(int kt)
+{
+  return kt == KS_GAUSSIAN || kt == KS_GAUSS_UNSCALED || kt == KS_GAUSSIAN_VAR_BANDWIDTH;
+}
+
+// Exponential kernels: K = 2^-(ahi + alo) of one pair (alo a small
+// correction).  Returns 1 for a pair the main epilogue flags for the FP64
+// recheck (same tests), 2 for a pair whose FP32 value may be off by more than
+// the per-pair budget once it is not negligible (the main epilogue drops those
+// as underflowed), 0 otherwise.
+template <int KT>
+__device__ __forceinline__ int exp_arg(float H, float L, const PtMeta &b, const PtMeta &am, float rc,
+                                       const TaskParam &T, bool exact, bool gfast, float &ahi, float &alo)
+{
+  if constexpr (KT == KS_GAUSSIAN) {
+    if (gfast) {
+      const float t1 = (am.n_hi + b.n_hi) - H, tt = t1 - L, ee = (t1 - tt) - L;
+      ahi = -tt * rc;                              // exact: -rc is a power of two
+      alo = -ee * rc;
+      return 0;
+    }
+  }
+  float t, lo, s;
+  if (exact) assemble<true>(H, L, am.n_hi, am.n_lo, b.n_hi, b.n_lo, rc, t, lo, s);
+  else assemble<false>(H, L, am.n_hi, am.n_lo, b.n_hi, b.n_lo, rc, t, lo, s);
+  const bool fl = T.any_flag != 0;
+  if constexpr (KT == KS_GAUSSIAN) {
+    ahi = t; alo = lo;
+    if (fl && (t < T.t_flag || t < T.rho * s)) return 1;
+    return T.t_flag > 0.f ? 2 : 0;
+  } else if constexpr (KT == KS_GAUSS_UNSCALED) {
+    const float fh = -T.s2, fl2 = -T.s2l;
+    ahi = t * fh; alo = fmaf(t, fh, -ahi) + fmaf(lo, fh, t * fl2);
+    if (fl && (t < T.t_flag || t < T.rho * s)) return 1;
+    return T.t_flag > 0.f ? 2 : 0;
+  } else {
+    const float fh = -am.h * b.h;                  // 0.5 log2(e) h_i h_j
+    const float fl2 = -(fmaf(am.h, b.h, fh) + fmaf(am.h, __int_as_float(b.pad[1]), __int_as_float(am.pad[1]) * b.h));
+    ahi = t * fh; alo = fmaf(t, fh, -ahi) + fmaf(lo, fh, t * fl2);
+    if (fl && fh > T.t_flag) return t * fh < 126.f ? 1 : 2;
+    return 0;
+  }
+}
+
+// A row whose kernel values over a tile's 32 columns all lie below 2^-96 is
+// summed again relative to its largest value 2^-M (FP32 flushes values below
+// 2^-126 to zero, FP64 keeps them): sum_j 2^(M - a_j) (1 - ln2 alo_j) w_j,
+// times 2^-M in FP64; pairs whose FP32 value is not accurate enough are
+// evaluated in FP64, and flagged pairs stay with the main recheck.  Rows of
+// the warp without `need` only take part in the TMEM loads.
+template <int KT>
+__device__ __noinline__ double rescue_exp(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp,
+                                          const PtMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
+                                          bool gfast, bool need)
+{
+  float M = 3.0e38f, sum = 0.f;
+  double dsum = 0.0;
+  for (int pass = 0; pass < 2; pass++) {
+    for (int half = 0; half < 2; half++) {
+      const int c0 = grp * 32 + half * 16;
+      uint32_t h[16], l[16];
+      tmem_ld16(tH + c0, h);
+      tmem_ld16(tH + 128 + c0, l);
+      tmem_ld_wait();
+      if (!need) continue;
+      for (int j = 0; j < 16; j++) {
+        const int c = c0 + j;
+        if (c >= ncols) break;
+        float ahi, alo;
+        const int r = exp_arg<KT>(__uint_as_float(h[j]), __uint_as_float(l[j]), bm[c], am, rc, T, exact, gfast,
+                                  ahi, alo);
+        if (pass == 0) {
+          if (r == 0) M = fminf(M, ahi);
+        } else if (r == 0) {
+          sum = fmaf(ex2_approx(M - ahi) * fmaf(-0.69314718f, alo, 1.0f), bm[c].w, sum);
+        } else if (r == 2) {
+          dsum += recheck64<KT>(a, T.kp, am.pos, bm[c].pos);
+        }
+      }
+    }
+  }
+  return dsum + ((M < 3.0e38f) ? (double)sum * exp2(-(double)M) : 0.0);
+}
+
+// One warp's share of one tile (32 columns of its 32 rows): TMEM loads, kernel
+// values, weighted sums, FP64 rechecks of the flagged pairs.  Returns the row
+// sum of these columns.
+template <int KT>
+__device__ __forceinline__ double tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
+                                                const PtMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
+                                                bool gfast, bool dump)
+{
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  double rchk = 0.0;
+#pragma unroll 1
+  for (int half = 0; half < 2; half++) {
+    const int c0 = grp * 32 + half * 16;
+    uint32_t h[16], l[16];
+    tmem_ld16(tH + c0, h);
+    tmem_ld16(tH + 128 + c0, l);
+    tmem_ld_wait();
+    if (dump) dump_chunk<KT, 16>(a.dump, row, c0, h, l, bm + c0, am, rc, T.kp);
+    if constexpr (KT == KS_GAUSSIAN) {
+      if (gfast) { epi_chunk_gfast<16>(h, l, bm + c0, am.n_hi, rc, acc); continue; }
+    }
+    if constexpr (kt_uses_norms(KT)) {
+      uint32_t flags = 0;
+      const bool fl = T.any_flag != 0;
+      if (exact) {
+        if (fl) flags = epi_chunk<KT, true, true, 16>(h, l, bm + c0, am, rc, T, acc);
+        else epi_chunk<KT, true, false, 16>(h, l, bm + c0, am, rc, T, acc);
+      } else {
+        if (fl) flags = epi_chunk<KT, false, true, 16>(h, l, bm + c0, am, rc, T, acc);
+        else epi_chunk<KT, false, false, 16>(h, l, bm + c0, am, rc, T, acc);
+      }
+      // FP64 rechecks of the flagged pairs of these 16 columns
+      while (flags) {
+        const int j = __ffs(flags) - 1;
+        flags &= flags - 1;
+        const int c = c0 + j;
+        if (c < ncols && am.pos >= 0) rchk += recheck64<KT>(a, T.kp, am.pos, bm[c].pos);
+      }
+    } else {
+      epi_chunk_ip<KT, 16>(h, l, bm + c0, ncols - c0, rc, T.kp, acc);
+    }
+  }
+  if constexpr (kt_exponential(KT)) {
+    // values below 2^-96 across the row's 32 columns (flagged pairs included)
+    const float W = __int_as_float(bm[grp * 32].pad[0]);
+    const bool need = am.pos >= 0 &&
+                      fabsf((acc[0] + acc[1]) + (acc[2] + acc[3])) + (float)fabs(rchk) < 0x1p-96f * W;
+    if (__any_sync(0xffffffffu, need)) {
+      const double r = rescue_exp<KT>(a, T, tH, grp, bm, ncols, am, rc, exact, gfast, need);
+      if (need) return rchk + r;
+    }
+  }
+  return rchk + (((double)acc[0] + (double)acc[1]) + ((double)acc[2] + (double)acc[3]));
+}
+
 template <int KT>
 __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
 {
@@ -613,7 +912,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
   volatile int *abort = &S->abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int items = a.ntm * a.nsc;
+  const int items = a.tab ? a.ntab : a.ntm * a.nsc;
 
   if (threadIdx.x == 0) {
     mbar_init(&S->a_full, 1);
@@ -645,9 +944,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       for (int s = 0; s < NMETA; s++) m_last[s] = -1;
       bool stop = false;
       for (int it = 0, item = blockIdx.x; item < items && !*abort && !stop; it++, item += gridDim.x) {
-        const int ti = item % a.ntm, sc = item / a.ntm;
+        const ItemGeo G = item_geo(a, item);
         if (it > 0 && !mbar_wait(&S->a_empty, (it - 1) & 1, abort, WAIT_LIMIT)) break;
-        const uint8_t *imgA = a.imgA + (size_t)ti * a_bytes;
+        const uint8_t *imgA = a.imgA + (size_t)G.ti * a_bytes;
         if (resident) {
           mbar_arrive_expect_tx(&S->a_full, (uint32_t)a_bytes);
           bulk_g2s(sA, imgA, (uint32_t)a_bytes, &S->a_full);
@@ -656,8 +955,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           bulk_g2s(sAmeta, imgA + a_op, (uint32_t)meta_bytes, &S->a_full);
         }
         a_issued = it;
-        const int t0 = sc * a.chunk_tiles, t1 = min(a.ntn, t0 + a.chunk_tiles);
-        for (int tj = t0; tj < t1 && !stop; tj++, tt++) {
+        for (int tj = G.t0; tj < G.t1 && !stop; tj++, tt++) {
           const uint8_t *imgB = a.imgB + (size_t)tj * b_bytes;
           for (int c = 0; c < L.nch; c++, g++) {
             const int st = g % L.nstage, u = g / L.nstage;
@@ -701,10 +999,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       int g = 0, tc = 0;
       bool stop = false;
       for (int it = 0, item = blockIdx.x; item < items && !*abort && !stop; it++, item += gridDim.x) {
-        const int sc = item / a.ntm;
+        const ItemGeo G = item_geo(a, item);
         if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
-        const int t0 = sc * a.chunk_tiles, t1 = min(a.ntn, t0 + a.chunk_tiles);
-        for (int tj = t0; tj < t1 && !stop; tj++, tc++) {
+        for (int tj = G.t0; tj < G.t1 && !stop; tj++, tc++) {
           const int buf = tc & 1;
           if (tc >= 2 && !mbar_wait(&S->t_empty[buf], ((tc >> 1) - 1) & 1, abort, WAIT_LIMIT)) { stop = true; break; }
           const uint32_t dH = tmem + buf * 256, dL = tmem + buf * 256 + 128;
@@ -747,62 +1044,55 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     const int row = qd * 32 + lane;
     const Params *P = a.P;
     const float rc = P->rc;
-    const bool flags_on = P->any_flag != 0, exact = P->exact_t1 != 0, gfast = P->gfast != 0;
+    const bool exact = P->exact_t1 != 0, gfast = P->gfast != 0;
+    TaskParam T0;                                  // the single call's parameters
+    if constexpr (KT != KS_LIST) {
+      T0.kp = a.kp; T0.t_flag = P->t_flag; T0.rho = P->rho; T0.s2 = T0.s2l = 0.f;
+      T0.c0h = P->c0h; T0.c0l = P->c0l; T0.any_flag = P->any_flag; T0.centred = P->centred;
+    }
     int g = 0, tc = 0;
     for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
-      const int ti = item % a.ntm, sc = item / a.ntm;
+      const ItemGeo G = item_geo(a, item);
+      TaskParam T;
+      if constexpr (KT == KS_LIST) T = a.tp[G.task];
+      else T = T0;
       if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
       const PtMeta am = ((const PtMeta *)sAmeta)[row];
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->a_empty);
       double racc = 0.0;
-      const int t0 = sc * a.chunk_tiles, t1 = min(a.ntn, t0 + a.chunk_tiles);
       bool ok = true;
-      for (int tj = t0; tj < t1; tj++, g++, tc++) {
+      for (int tj = G.t0; tj < G.t1; tj++, g++, tc++) {
         const int ms = g % NMETA, buf = tc & 1;
         if (!mbar_wait(&S->t_full[buf], (tc >> 1) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
         if (!mbar_wait(&S->m_full[ms], (g / NMETA) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
         tc_fence_after();
         const PtMeta *bm = (const PtMeta *)(sBm + ms * meta_bytes);
-        const int ncols = min(BN, a.n - tj * BN);
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        const int ncols = a.tab ? a.btile_cols[tj] : min(BN, a.n - tj * BN);
         const uint32_t tH = tmem + ((uint32_t)(qd * 32) << 16) + buf * 256;
-#pragma unroll 1
-        for (int half = 0; half < 2; half++) {
-          const int c0 = grp * 32 + half * 16;
-          uint32_t h[16], l[16];
-          tmem_ld16(tH + c0, h);
-          tmem_ld16(tH + 128 + c0, l);
-          tmem_ld_wait();
-          if constexpr (KT == KS_GAUSSIAN) {
-            if (gfast) {
-              epi_chunk_gfast<16>(h, l, bm + c0, am.n_hi, rc, acc);
-              if (a.dump && blockIdx.x == 0 && tc == 0) dump_chunk<KT, 16>(a.dump, row, c0, h, l, bm + c0, am, rc, a.kp);
-              continue;
-            }
+        const bool dump = a.dump && blockIdx.x == 0 && tc == 0;
+        if constexpr (KT == KS_LIST) {
+          switch (T.kp.type) {
+            case KS_GAUSSIAN:
+              racc += tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+            case KS_GAUSSIAN_VAR_BANDWIDTH:
+              racc += tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+            case KS_POLYNOMIAL:
+              racc += tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+            case KS_LAPLACE:
+              racc += tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+            case KS_TANH:
+              racc += tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+            case KS_QUARTIC:
+              racc += tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+            case KS_MULTIQUADRATIC:
+              racc += tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+            default:
+              racc += tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
           }
-          if constexpr (kt_uses_norms(KT)) {
-            uint32_t flags = 0;
-            if (exact) {
-              if (flags_on) flags = epi_chunk<KT, true, true, 16>(h, l, bm + c0, am, rc, P, a.kp, acc);
-              else epi_chunk<KT, true, false, 16>(h, l, bm + c0, am, rc, P, a.kp, acc);
-            } else {
-              if (flags_on) flags = epi_chunk<KT, false, true, 16>(h, l, bm + c0, am, rc, P, a.kp, acc);
-              else epi_chunk<KT, false, false, 16>(h, l, bm + c0, am, rc, P, a.kp, acc);
-            }
-            // FP64 rechecks of the flagged pairs of these 16 columns
-            while (flags) {
-              const int j = __ffs(flags) - 1;
-              flags &= flags - 1;
-              const int c = c0 + j;
-              if (c < ncols && am.pos >= 0) racc += recheck64<KT>(a, am.pos, bm[c].pos);
-            }
-          } else {
-            epi_chunk_ip<KT, 16>(h, l, bm + c0, ncols - c0, rc, a.kp, acc);
-          }
-          if (a.dump && blockIdx.x == 0 && tc == 0) dump_chunk<KT, 16>(a.dump, row, c0, h, l, bm + c0, am, rc, a.kp);
+        } else {
+          racc += tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump);
         }
-        racc += ((double)acc[0] + (double)acc[1]) + ((double)acc[2] + (double)acc[3]);
         tc_fence_before();
         __syncwarp();
         if (lane == 0) { mbar_arrive(&S->t_empty[buf]); mbar_arrive(&S->m_empty[ms]); }
@@ -814,9 +1104,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");
       if (grp == 0) {
         for (int q = 0; q < EPI_GROUPS - 1; q++) racc += xs[q][row];
-        const int grow = ti * BM + row;
         if (KT == KS_GAUSSIAN && gfast) racc *= (double)am.h;   // the row's low-norm factor
-        if (grow < a.m) a.partial[(size_t)sc * a.ldp + grow] = racc;
+        if (row < G.rows) a.partial[G.out + row] = racc;
       }
     }
   }
@@ -863,6 +1152,7 @@ cudaError_t launch_tiles(const TileArgs &a, int grid, size_t smem, cudaStream_t 
     case KS_TANH: return launch_tiles_t<KS_TANH>(a, grid, smem, s);
     case KS_QUARTIC: return launch_tiles_t<KS_QUARTIC>(a, grid, smem, s);
     case KS_MULTIQUADRATIC: return launch_tiles_t<KS_MULTIQUADRATIC>(a, grid, smem, s);
+    case KS_LIST: return launch_tiles_t<KS_LIST>(a, grid, smem, s);
     default: return launch_tiles_t<KS_EPANECHNIKOV>(a, grid, smem, s);
   }
 }
@@ -888,7 +1178,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
                   cudaStream_t s, bool stream_ordered_alloc)
 {
   using namespace split;
-  (void)XA2; (void)XB2; (void)nxa; (void)nxb;
+  (void)XA2; (void)XB2;
   // padded k: a multiple of the MMA k-step (16) up to one chunk, of the chunk beyond
   const int kpad = k <= KCH ? (k + 15) / 16 * 16 : (k + KCH - 1) / KCH * KCH;
   if (kpad > 1024) return GSKS_ERR_TOO_LARGE;   // the exact head accumulation needs k <= 1024
@@ -928,17 +1218,21 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   {
     const long long tot = (long long)(m + n) * k;
     const int blocks = (int)std::min<long long>(4LL * sms, std::max<long long>(1, (tot + 255) / 256));
-    bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(m, n, k, XA, amap, XB, bmap, bbox);
+    bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(m, n, k, XA, amap, nxa, XB, bmap, nxb,
+                                                               (int *)c->err.p, bbox);
   }
   params_kernel<<<1, 1024, 0, s>>>(k, ker->type, ker->scal, ker->powe, tau, bbox, centre, P);
-  pack_kernel<<<ntm, BM, 0, s>>>(0, m, k, kpad, XA, amap, nullptr, nullptr, hi, ker->type, centre, P, ws + o_a);
-  pack_kernel<<<ntn, BN, 0, s>>>(1, n, k, kpad, XB, bmap, w, wmap, hj, ker->type, centre, P, ws + o_b);
+  pack_kernel<<<ntm, BM, 0, s>>>(0, m, k, kpad, XA, amap, nxa, (int *)c->err.p, nullptr, nullptr, hi, ker->type,
+                                 centre, P, ws + o_a, nullptr, nullptr, nullptr);
+  pack_kernel<<<ntn, BN, 0, s>>>(1, n, k, kpad, XB, bmap, nxb, (int *)c->err.p, w, wmap, hj, ker->type, centre,
+                                 P, ws + o_b, nullptr, nullptr, nullptr);
 
   TileArgs a{};
   a.m = m; a.n = n; a.k = k; a.kpad = kpad; a.kt = ker->type;
   a.ntm = ntm; a.ntn = ntn; a.nsc = nsc; a.chunk_tiles = chunk_tiles;
   a.imgA = ws + o_a; a.imgB = ws + o_b;
   a.XA = XA; a.XB = XB; a.amap = amap; a.bmap = bmap; a.wmap = wmap; a.w = w;
+  a.nxa = nxa; a.nxb = nxb;
   a.hi = hi; a.hj = hj;
   a.kp = make_kparams(ker, hi, hj);
   a.kp.coinc = coincidence_eps(k);
@@ -960,6 +1254,138 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   if (stream_ordered_alloc) cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_status(e, "split launch");
   note_launches(7);
+  return GSKS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Split-precision form of dgsks_list.  Every task's targets and sources are
+// packed into tiles of their own (tile images carry the task's centring and
+// bandwidths); a work item is (task, target tile, up to chunk / BN source
+// tiles), and every item writes the row sums of its chunk to
+// partial[pbase[t] + sc * m_t + r], the layout the list merge reads.  One
+// bounding box, hence one scale and one centre, covers all tasks, and the
+// per-task flag thresholds come from it.
+int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
+                       const long long *pbase, int chunk, const double *XA, const int *a_idx, int nxa,
+                       const double *XB, const int *b_idx, int nxb, const double *w, const int *w_idx,
+                       double *partial, cudaStream_t s, int *launches)
+{
+  using namespace split;
+  if (chunk % BN) return GSKS_ERR_ARG;
+  const int kpad = k <= KCH ? (k + 15) / 16 * 16 : (k + KCH - 1) / KCH * KCH;
+  if (kpad > 1024) return GSKS_ERR_TOO_LARGE;
+  const int chunk_tiles = chunk / BN;
+
+  // tiles and items on the host
+  std::vector<int2> ta, tb;
+  std::vector<int> ta_task, tb_task, tb_cols;
+  std::vector<SplitItem> items;
+  std::vector<double> cost;
+  long long na = 0, nb = 0;
+  for (int t = 0; t < ntask; t++) {
+    const int m = hoff_a[t + 1] - hoff_a[t], n = hoff_b[t + 1] - hoff_b[t];
+    if (m <= 0 || n <= 0) continue;
+    na += m; nb += n;
+    const int a_base = (int)ta.size(), b_base = (int)tb.size();
+    for (int i0 = 0; i0 < m; i0 += BM) { ta.push_back(make_int2(hoff_a[t] + i0, std::min(BM, m - i0))); ta_task.push_back(t); }
+    for (int j0 = 0; j0 < n; j0 += BN) {
+      tb.push_back(make_int2(hoff_b[t] + j0, std::min(BN, n - j0)));
+      tb_task.push_back(t);
+      tb_cols.push_back(std::min(BN, n - j0));
+    }
+    const int ntn = (int)tb.size() - b_base;
+    // relative epilogue cost per tile: the Laplace powering dominates
+    const double wkt = kps[t].type == KS_LAPLACE ? 4.0 : 1.0;
+    for (int sc = 0; sc * chunk_tiles < ntn; sc++)
+      for (int i0 = 0; i0 < m; i0 += BM) {
+        SplitItem it{};
+        it.a_tile = a_base + i0 / BM;
+        it.b0 = b_base + sc * chunk_tiles;
+        it.b1 = b_base + std::min(ntn, (sc + 1) * chunk_tiles);
+        it.task = t;
+        it.out = pbase[t] + (long long)sc * m + i0;
+        it.rows = std::min(BM, m - i0);
+        items.push_back(it);
+        cost.push_back(wkt * (it.b1 - it.b0));
+      }
+  }
+  if (items.empty()) return GSKS_OK;
+  {
+    std::vector<int> ord(items.size());
+    for (size_t i = 0; i < ord.size(); i++) ord[i] = (int)i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+    std::vector<SplitItem> sorted(items.size());
+    for (size_t i = 0; i < ord.size(); i++) sorted[i] = items[ord[i]];
+    items.swap(sorted);
+  }
+  if (na > INT32_MAX || nb > INT32_MAX) return GSKS_ERR_TOO_LARGE;
+
+  auto al = [](size_t x) { return (x + 1023) & ~(size_t)1023; };
+  const size_t o_params = 0;
+  const size_t o_centre = al(sizeof(Params));
+  const size_t o_bbox = o_centre + al((size_t)k * 8);
+  const size_t o_ta = o_bbox + al((size_t)2 * k * 8);
+  const size_t o_tat = o_ta + al(ta.size() * sizeof(int2));
+  const size_t o_tb = o_tat + al(ta.size() * sizeof(int));
+  const size_t o_tbt = o_tb + al(tb.size() * sizeof(int2));
+  const size_t o_tbc = o_tbt + al(tb.size() * sizeof(int));
+  const size_t o_items = o_tbc + al(tb.size() * sizeof(int));
+  const size_t o_kps = o_items + al(items.size() * sizeof(SplitItem));
+  const size_t o_tp = o_kps + al((size_t)ntask * sizeof(KParams));
+  const size_t o_a = o_tp + al((size_t)ntask * sizeof(TaskParam));
+  const size_t o_b = o_a + al(ta.size() * tile_bytes(BM, kpad));
+  const size_t total = o_b + al(tb.size() * tile_bytes(BN, kpad));
+  if (!c->dwork.ensure(total)) return GSKS_ERR_ALLOC;
+  uint8_t *ws = (uint8_t *)c->dwork.p;
+  Params *P = (Params *)(ws + o_params);
+  double *centre = (double *)(ws + o_centre);
+  long long *bbox = (long long *)(ws + o_bbox);
+  TaskParam *tp = (TaskParam *)(ws + o_tp);
+  auto up = [&](size_t off, const void *src, size_t bytes) {
+    return bytes == 0 || cudaMemcpyAsync(ws + off, src, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  };
+  if (!(up(o_ta, ta.data(), ta.size() * sizeof(int2)) && up(o_tat, ta_task.data(), ta_task.size() * sizeof(int)) &&
+        up(o_tb, tb.data(), tb.size() * sizeof(int2)) && up(o_tbt, tb_task.data(), tb_task.size() * sizeof(int)) &&
+        up(o_tbc, tb_cols.data(), tb_cols.size() * sizeof(int)) &&
+        up(o_items, items.data(), items.size() * sizeof(SplitItem)) &&
+        up(o_kps, kps, (size_t)ntask * sizeof(KParams))))
+    return cuda_status(cudaGetLastError(), "split list tables");
+
+  const float tau = 5e-7f;
+  const int sms = std::max(1, c->num_sms);
+  int *err = (int *)c->err.p;
+  bbox_init<<<1, 256, 0, s>>>(k, bbox);
+  {
+    // every list position (tasks with an empty side included: harmless)
+    const int ma = hoff_a[ntask], mb = hoff_b[ntask];
+    const long long tot = ((long long)ma + mb) * k;
+    const int blocks = (int)std::min<long long>(4LL * sms, std::max<long long>(1, (tot + 255) / 256));
+    bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(ma, mb, k, XA, a_idx, nxa, XB, b_idx, nxb, err, bbox);
+  }
+  params_kernel<<<1, 1024, 0, s>>>(k, KS_LIST, 0.0, 0.0, tau, bbox, centre, P);
+  task_params_kernel<<<(ntask + 127) / 128, 128, 0, s>>>(ntask, (const KParams *)(ws + o_kps), P, tau, tp);
+  pack_kernel<<<(int)ta.size(), BM, 0, s>>>(0, 0, k, kpad, XA, a_idx, nxa, err, nullptr, nullptr, nullptr, KS_LIST,
+                                            centre, P, ws + o_a, (const int2 *)(ws + o_ta),
+                                            (const int *)(ws + o_tat), tp);
+  pack_kernel<<<(int)tb.size(), BN, 0, s>>>(1, 0, k, kpad, XB, b_idx, nxb, err, w, w_idx, nullptr, KS_LIST,
+                                            centre, P, ws + o_b, (const int2 *)(ws + o_tb),
+                                            (const int *)(ws + o_tbt), tp);
+  TileArgs a{};
+  a.k = k; a.kpad = kpad; a.kt = KS_LIST;
+  a.imgA = ws + o_a; a.imgB = ws + o_b;
+  a.XA = XA; a.XB = XB; a.amap = a_idx; a.bmap = b_idx; a.wmap = w_idx; a.w = w;
+  a.nxa = nxa; a.nxb = nxb;
+  a.P = P;
+  a.partial = partial;
+  a.err = err;
+  a.tab = (const SplitItem *)(ws + o_items);
+  a.ntab = (int)items.size();
+  a.tp = tp;
+  a.btile_cols = (const int *)(ws + o_tbc);
+  const int grid = std::min((int)items.size(), sms);
+  cudaError_t e = launch_tiles(a, grid, smem_bytes(kpad), s);
+  if (e != cudaSuccess) return cuda_status(e, "split list launch");
+  *launches += 7;
   return GSKS_OK;
 }
 

@@ -128,3 +128,44 @@ def test_split_mixture_with_duplicates(gpu, oracle_mod, k):
     assert e["normwise"] <= TOL and e["cond_max"] <= TOL, ("gaussian", e)
     e = _run(gpu, oracle_mod, 1, dict(scal=1.0 / k, cons=1.0, powe=2.0), X, w, amap, bmap, umap, wmap)
     assert e["cond_max"] <= TOL, ("polynomial", e)
+
+
+def _separated(seed, N, k, src_box, tgt_box, m, n):
+    """Sources in the cube src_box^k, targets in tgt_box^k: every kernel value of
+    a narrow Gaussian between them lies far below the FP32 range."""
+    rng = np.random.default_rng(seed)
+    X = np.empty((N, k))
+    half = N // 2
+    X[:half] = rng.uniform(*src_box, (half, k))
+    X[half:] = rng.uniform(*tgt_box, (N - half, k))
+    w = rng.standard_normal(N)
+    bmap = rng.choice(half, n, replace=False).astype(np.int32)
+    amap = (half + rng.choice(N - half, m, replace=False)).astype(np.int32)
+    umap = rng.permutation(N)[:m].astype(np.int32)
+    wmap = rng.permutation(N)[:n].astype(np.int32)
+    return X, w, amap, bmap, umap, wmap
+
+
+def test_split_gaussian_below_fp32_range_rescaled(gpu, oracle_mod):
+    """K between 1e-41 and 1e-63 (FP64 normal, FP32 zero) with a distance bound
+    tight enough for FP32 values: rows are summed relative to their largest value."""
+    case = _separated(7, 4000, 3, (0.0, 0.1), (0.9, 1.0), 600, 900)
+    e = _run(gpu, oracle_mod, 0, dict(scal=-48.5), *case)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+def test_split_gaussian_below_fp32_range_fp64(gpu, oracle_mod):
+    """K near 1e-170 with a loose distance bound: those rows go to FP64."""
+    case = _separated(8, 4000, 16, (0.0, 0.3), (0.7, 1.0), 500, 700)
+    e = _run(gpu, oracle_mod, 0, dict(scal=-100.0), *case)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+def test_split_var_bandwidth_narrow(gpu, oracle_mod):
+    """Bandwidth products up to 2500 (h down to 0.02): the pairs whose FP32
+    value is not accurate enough are recomputed in FP64."""
+    X, w, amap, bmap, umap, wmap = _case(9, 4000, 8, 700, 900)
+    rng = np.random.default_rng(45)
+    h = np.exp(rng.uniform(np.log(0.02), np.log(0.7), X.shape[0]))
+    e = _run(gpu, oracle_mod, 3, {}, X, w, amap, bmap, umap, wmap, hi=1.0 / h ** 2)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e

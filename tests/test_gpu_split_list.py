@@ -1,0 +1,140 @@
+"""dgsks_list in the split-precision tensor-core form against the oracle's list
+restatement: mixed per-task kernels (Gaussian of several bandwidths, Laplace,
+polynomial, variable-bandwidth Gaussian), uneven and empty tasks, separate u
+and w maps, host and device arrays, streamed k.
+
+Gate as for the single call: normwise error and the conditioned max-relative
+error max_e |du_e| / sum |K w| over the list positions naming u entry e,
+both within 1e-6."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+SPLIT = 1
+
+
+def _lists(rng, N, sizes_a, sizes_b):
+    a_idx = np.concatenate([rng.permutation(N)[:s] for s in sizes_a]).astype(np.int32)
+    b_idx = np.concatenate([rng.permutation(N)[:s] for s in sizes_b]).astype(np.int32)
+    a_off = np.concatenate([[0], np.cumsum(sizes_a)]).astype(np.int32)
+    b_off = np.concatenate([[0], np.cumsum(sizes_b)]).astype(np.int32)
+    return a_off, a_idx, b_off, b_idx
+
+
+def _cond(O, kers, a_off, a_idx, u_idx, b_off, b_idx, w_idx, X, X2, w, nu):
+    """sum over list positions naming each u entry of sum_j |K w| (oracle rows)."""
+    cond = np.zeros(nu)
+    for t in range(a_off.size - 1):
+        a0, a1, b0, b1 = a_off[t], a_off[t + 1], b_off[t], b_off[t + 1]
+        if a1 == a0 or b1 == b0:
+            continue
+        _, c = O.rows(kers[t], np.arange(a1 - a0, dtype=np.int32), X, X2, a_idx[a0:a1], X, X2, b_idx[b0:b1],
+                      w, w_idx[b0:b1])
+        np.add.at(cond, u_idx[a0:a1], c)
+    return cond
+
+
+def _specs(rng, ntask, k, mix, X=None):
+    out = []
+    for t in range(ntask):
+        c = mix[t % len(mix)]
+        if c == "gauss":
+            out.append((0, dict(scal=-1.0 / (2 * rng.uniform(0.1, 2.0) ** 2))))
+        elif c == "laplace":
+            out.append((2, {}))
+        elif c == "poly":
+            out.append((1, dict(scal=1.0 / k, cons=1.0, powe=float(2 + t % 2))))
+        elif c == "varbw":
+            out.append((3, {}))
+    return out
+
+
+def _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device, hvec=None):
+    from ks_gb300 import gsks
+    torch = gpu
+    N = X.shape[0]
+    X2 = O.norms(X)
+    kw_o = [dict(p) for _, p in specs]
+    kw_g = [dict(p) for _, p in specs]
+    hd = torch.from_numpy(hvec).cuda() if (hvec is not None and device) else hvec
+    for (t, _), ko, kg in zip(specs, kw_o, kw_g):
+        if t == 3:
+            ko.update(hi=hvec, hj=hvec)
+            kg.update(hi=hd, hj=hd)
+    kers_o = [O.make_kernel(t, **p) for (t, _), p in zip(specs, kw_o)]
+    kers_g = [gsks.make_kernel(t, **p) for (t, _), p in zip(specs, kw_g)]
+    u_ref = np.zeros(N)
+    O.dgsks_list(kers_o[0], u_ref, a_off, a_idx, u_idx, b_off, b_idx, w_idx, X, X2, X, X2, w, kers=kers_o)
+    cond = _cond(O, kers_o, a_off, a_idx, u_idx, b_off, b_idx, w_idx, X, X2, w, N)
+    prev = gsks.get_precision()
+    gsks.set_precision(SPLIT)
+    try:
+        if device:
+            t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+            u = torch.zeros(N, dtype=torch.float64, device="cuda")
+            gsks.dgsks_list(kers_g[0], u, t(a_off), t(a_idx), t(b_off), t(b_idx), t(X), None, t(X), None, t(w),
+                            u_idx=t(u_idx), w_idx=t(w_idx), kers=kers_g)
+            torch.cuda.synchronize()
+            got = u.cpu().numpy()
+        else:
+            got = np.zeros(N)
+            gsks.dgsks_list(kers_g[0], got, a_off, a_idx, b_off, b_idx, X, X2, X, X2, w, u_idx=u_idx, w_idx=w_idx,
+                            kers=kers_g)
+        assert gsks.last_launch_count() > 0
+    finally:
+        gsks.set_precision(prev)
+    named = np.unique(u_idx)
+    return got, O.errors(got[named], u_ref[named], cond=cond[named])
+
+
+def test_split_list_mixed_kernels_host(gpu, oracle_mod):
+    O = oracle_mod
+    rng = np.random.default_rng(11)
+    N, k, ntask = 6000, 16, 60
+    X = rng.random((N, k)); w = rng.standard_normal(N)
+    sa = rng.integers(0, 700, ntask); sb = rng.integers(0, 700, ntask)
+    sa[3] = 0; sb[7] = 0                       # empty tasks
+    a_off, a_idx, b_off, b_idx = _lists(rng, N, sa, sb)
+    u_idx = np.concatenate([rng.permutation(N)[:s] for s in sa]).astype(np.int32)
+    w_idx = rng.integers(0, N, b_idx.size).astype(np.int32)
+    specs = _specs(rng, ntask, k, ["gauss", "laplace", "poly"])
+    got, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=False)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+    # deterministic across runs
+    got2, _ = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=False)
+    assert np.array_equal(got, got2)
+
+
+def test_split_list_device_var_bandwidth(gpu, oracle_mod):
+    O = oracle_mod
+    rng = np.random.default_rng(12)
+    N, k, ntask = 5000, 8, 24
+    X = rng.random((N, k)); w = rng.standard_normal(N)
+    hvec = np.exp(rng.uniform(np.log(2.0), np.log(50.0), N))    # 1 / h^2 for h in [0.14, 0.7]
+    sa = rng.integers(1, 900, ntask); sb = rng.integers(1, 1500, ntask)
+    a_off, a_idx, b_off, b_idx = _lists(rng, N, sa, sb)
+    u_idx = a_idx.copy(); w_idx = b_idx.copy()
+    # per task distinct targets: u entries shared across tasks only
+    specs = _specs(rng, ntask, k, ["varbw", "gauss"])
+    _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True, hvec=hvec)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+@pytest.mark.parametrize("k", [3, 64, 100])
+def test_split_list_log_uniform_sizes(gpu, oracle_mod, k):
+    """Task sizes log-uniform in [32, 4096] (the batched workload's distribution,
+    fewer tasks), Gaussian h in [0.1, 2], Laplace, polynomial of power 2 or 3."""
+    O = oracle_mod
+    rng = np.random.default_rng(100 + k)
+    N, ntask = 20000, 40
+    X = rng.random((N, k)); w = rng.standard_normal(N)
+    sa = np.exp(rng.uniform(np.log(32), np.log(4096), ntask)).astype(int)
+    sb = np.exp(rng.uniform(np.log(32), np.log(4096), ntask)).astype(int)
+    a_off, a_idx, b_off, b_idx = _lists(rng, N, sa, sb)
+    u_idx = a_idx.copy(); w_idx = b_idx.copy()
+    kinds = ["gauss", "laplace", "poly"] if k > 2 else ["gauss", "poly"]
+    specs = _specs(rng, ntask, k, kinds)
+    _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
