@@ -759,95 +759,20 @@ __host__ __device__ constexpr bool kt_exponential(int kt)
   return kt == KS_GAUSSIAN || kt == KS_GAUSS_UNSCALED || kt == KS_GAUSSIAN_VAR_BANDWIDTH;
 }
 
-// Exponential kernels: K = 2^-(ahi + alo) of one pair (alo a small
-// correction).  Returns 1 for a pair the main epilogue flags for the FP64
-// recheck (same tests), 2 for a pair whose FP32 value may be off by more than
-// the per-pair budget once it is not negligible (the main epilogue drops those
-// as underflowed), 0 otherwise.
-template <int KT>
-__device__ __forceinline__ int exp_arg(float H, float L, const PtMeta &b, const PtMeta &am, float rc,
-                                       const TaskParam &T, bool exact, bool gfast, float &ahi, float &alo)
-{
-  if constexpr (KT == KS_GAUSSIAN) {
-    if (gfast) {
-      const float t1 = (am.n_hi + b.n_hi) - H, tt = t1 - L, ee = (t1 - tt) - L;
-      ahi = -tt * rc;                              // exact: -rc is a power of two
-      alo = -ee * rc;
-      return 0;
-    }
-  }
-  float t, lo, s;
-  if (exact) assemble<true>(H, L, am.n_hi, am.n_lo, b.n_hi, b.n_lo, rc, t, lo, s);
-  else assemble<false>(H, L, am.n_hi, am.n_lo, b.n_hi, b.n_lo, rc, t, lo, s);
-  const bool fl = T.any_flag != 0;
-  if constexpr (KT == KS_GAUSSIAN) {
-    ahi = t; alo = lo;
-    if (fl && (t < T.t_flag || t < T.rho * s)) return 1;
-    return T.t_flag > 0.f ? 2 : 0;
-  } else if constexpr (KT == KS_GAUSS_UNSCALED) {
-    const float fh = -T.s2, fl2 = -T.s2l;
-    ahi = t * fh; alo = fmaf(t, fh, -ahi) + fmaf(lo, fh, t * fl2);
-    if (fl && (t < T.t_flag || t < T.rho * s)) return 1;
-    return T.t_flag > 0.f ? 2 : 0;
-  } else {
-    const float fh = -am.h * b.h;                  // 0.5 log2(e) h_i h_j
-    const float fl2 = -(fmaf(am.h, b.h, fh) + fmaf(am.h, __int_as_float(b.pad[1]), __int_as_float(am.pad[1]) * b.h));
-    ahi = t * fh; alo = fmaf(t, fh, -ahi) + fmaf(lo, fh, t * fl2);
-    if (fl && fh > T.t_flag) return t * fh < 126.f ? 1 : 2;
-    return 0;
-  }
-}
-
-// A row whose kernel values over a tile's 32 columns all lie below 2^-96 is
-// summed again relative to its largest value 2^-M (FP32 flushes values below
-// 2^-126 to zero, FP64 keeps them): sum_j 2^(M - a_j) (1 - ln2 alo_j) w_j,
-// times 2^-M in FP64; pairs whose FP32 value is not accurate enough are
-// evaluated in FP64, and flagged pairs stay with the main recheck.  Rows of
-// the warp without `need` only take part in the TMEM loads.
-template <int KT>
-__device__ __noinline__ double rescue_exp(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp,
-                                          const PtMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
-                                          bool gfast, bool need)
-{
-  float M = 3.0e38f, sum = 0.f;
-  double dsum = 0.0;
-  for (int pass = 0; pass < 2; pass++) {
-    for (int half = 0; half < 2; half++) {
-      const int c0 = grp * 32 + half * 16;
-      uint32_t h[16], l[16];
-      tmem_ld16(tH + c0, h);
-      tmem_ld16(tH + 128 + c0, l);
-      tmem_ld_wait();
-      if (!need) continue;
-      for (int j = 0; j < 16; j++) {
-        const int c = c0 + j;
-        if (c >= ncols) break;
-        float ahi, alo;
-        const int r = exp_arg<KT>(__uint_as_float(h[j]), __uint_as_float(l[j]), bm[c], am, rc, T, exact, gfast,
-                                  ahi, alo);
-        if (pass == 0) {
-          if (r == 0) M = fminf(M, ahi);
-        } else if (r == 0) {
-          sum = fmaf(ex2_approx(M - ahi) * fmaf(-0.69314718f, alo, 1.0f), bm[c].w, sum);
-        } else if (r == 2) {
-          dsum += recheck64<KT>(a, T.kp, am.pos, bm[c].pos);
-        }
-      }
-    }
-  }
-  return dsum + ((M < 3.0e38f) ? (double)sum * exp2(-(double)M) : 0.0);
-}
-
 // One warp's share of one tile (32 columns of its 32 rows): TMEM loads, kernel
-// values, weighted sums, FP64 rechecks of the flagged pairs.  Returns the row
-// sum of these columns.
+// values, weighted sums, FP64 rechecks of the flagged pairs.  Adds the row
+// sum of these columns to racc.  The 32 columns are summed in FP32 (four
+// interleaved partial sums) and enter the FP64 row sum with one conversion and
+// one add: FP64 instructions issue at a small fraction of the FP32 rate here.
 template <int KT>
-__device__ __forceinline__ double tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
-                                                const PtMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
-                                                bool gfast, bool dump)
+__device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
+                                              const PtMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
+                                              bool gfast, bool dump, double &racc)
 {
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   double rchk = 0.0;
+  float fchk = 0.f;                 // |rechecked values|, for the underflow test
+  bool nchk = false;
 #pragma unroll 1
   for (int half = 0; half < 2; half++) {
     const int c0 = grp * 32 + half * 16;
@@ -874,23 +799,36 @@ __device__ __forceinline__ double tile_epilogue(const TileArgs &a, const TaskPar
         const int j = __ffs(flags) - 1;
         flags &= flags - 1;
         const int c = c0 + j;
-        if (c < ncols && am.pos >= 0) rchk += recheck64<KT>(a, T.kp, am.pos, bm[c].pos);
+        if (c < ncols && am.pos >= 0) {
+          const double v = recheck64<KT>(a, T.kp, am.pos, bm[c].pos);
+          rchk += v;
+          fchk += fabsf((float)v);
+          nchk = true;
+        }
       }
     } else {
       epi_chunk_ip<KT, 16>(h, l, bm + c0, ncols - c0, rc, T.kp, acc);
     }
   }
+  const float fs = (acc[0] + acc[1]) + (acc[2] + acc[3]);
   if constexpr (kt_exponential(KT)) {
-    // values below 2^-96 across the row's 32 columns (flagged pairs included)
+    // A row whose kernel values over these 32 columns all lie below 2^-96
+    // (FP32 flushes values below 2^-126 to zero, FP64 keeps them down to
+    // 2^-1074) takes these pairs from FP64 instead, flagged pairs included.
     const float W = __int_as_float(bm[grp * 32].pad[0]);
-    const bool need = am.pos >= 0 &&
-                      fabsf((acc[0] + acc[1]) + (acc[2] + acc[3])) + (float)fabs(rchk) < 0x1p-96f * W;
-    if (__any_sync(0xffffffffu, need)) {
-      const double r = rescue_exp<KT>(a, T, tH, grp, bm, ncols, am, rc, exact, gfast, need);
-      if (need) return rchk + r;
+    if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W) {
+      double r = 0.0;
+      const int c1 = min(grp * 32 + 32, ncols);
+      for (int c = grp * 32; c < c1; c++) r += recheck64<KT>(a, T.kp, am.pos, bm[c].pos);
+      if constexpr (KT == KS_GAUSSIAN) {
+        if (gfast) r /= (double)am.h;   // the caller applies the row factor to the row sum
+      }
+      racc += r;
+      return;
     }
   }
-  return rchk + (((double)acc[0] + (double)acc[1]) + ((double)acc[2] + (double)acc[3]));
+  racc += (double)fs;
+  if (nchk) racc += rchk;
 }
 
 template <int KT>
@@ -1074,24 +1012,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         if constexpr (KT == KS_LIST) {
           switch (T.kp.type) {
             case KS_GAUSSIAN:
-              racc += tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              racc += tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
             case KS_POLYNOMIAL:
-              racc += tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
             case KS_LAPLACE:
-              racc += tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
             case KS_TANH:
-              racc += tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
             case KS_QUARTIC:
-              racc += tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
             case KS_MULTIQUADRATIC:
-              racc += tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
             default:
-              racc += tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump); break;
+              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
           }
         } else {
-          racc += tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump);
+          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, racc);
         }
         tc_fence_before();
         __syncwarp();
