@@ -59,6 +59,7 @@ constexpr int BM = 128;             // targets per tile (TMEM lanes)
 constexpr int BN = 128;             // sources per tile
 constexpr int KPAD_MAX = 64;        // padded k of the target-resident kernel
 constexpr int NSTAGE = 3;           // source-tile operand stages
+constexpr int LTAB = 256;           // Laplace log2 table entries
 constexpr int NMETA = 4;            // source-tile metadata ring
 constexpr int NBLK = 3;             // slices per operand
 constexpr int EPI_GROUPS = 4;          // column groups of the epilogue
@@ -76,6 +77,13 @@ struct PtMeta {          // 32 bytes per point, appended to each tile image
                          // [1] var-bandwidth: low part of h (float bits)
 };
 
+// Laplace: K = scal d2^powe = 2^(log2 scal + powe log2 d2), powe = -P/2,
+// log2 scal = ls13 2^-13 + lsf.
+struct LapParam {
+  int P, ls13;
+  float lsf, mh;         // mh = -P/2
+};
+
 struct Params {          // per call, computed on the device
   double alpha, sigma, inv_sigma, q;
   double g;              // 2 sigma^2 2^-14: d2 = g (nu_i + nu_j - H - L)
@@ -86,7 +94,7 @@ struct Params {          // per call, computed on the device
   int any_flag;          // some pair may be flagged
   int exact_t1;          // nu_i + nu_j - H is exact in FP32
   int gfast;             // Gaussian without flags: low norm parts folded into w / row factors
-  float c0h, c0l;        // Laplace: scal^(1/m), m = -powe, as a double-float
+  LapParam lap;          // Laplace exponent constants
   double delta;          // absolute error bound of the assembled d2 (scaled units)
 };
 
@@ -100,7 +108,7 @@ struct TaskParam {
   KParams kp;
   float t_flag, rho;     // flag pairs with t < t_flag or t < rho * (n_i + n_j)
   float s2, s2l;         // Gaussian of the list form: scal * log2(e) = s2 + s2l
-  float c0h, c0l;        // Laplace: scal^(1/m), m = -powe
+  LapParam lap;          // Laplace
   int any_flag;
   int centred;           // distance kernels: coordinates taken relative to the centre
 };
@@ -218,6 +226,18 @@ __global__ void bbox_kernel(int m, int n, int k, const double *__restrict__ XA, 
   }
 }
 
+__device__ LapParam lap_param(double scal, double powe)
+{
+  LapParam L;
+  L.P = (int)rint(-2.0 * powe);
+  const double ls = log2(scal);
+  const double l13 = fmin(fmax(floor(ls * 8192.0), -0x1p30), 0x1p30);   // scal beyond the FP64 range: clamped
+  L.ls13 = (int)l13;
+  L.lsf = (float)(ls - l13 / 8192.0);
+  L.mh = -0.5f * (float)L.P;
+  return L;
+}
+
 // Centre, scales and the flag thresholds from the bounding box (one block).
 // kt = KS_LIST: the list form, whose tasks mix centred (distance) and
 // uncentred (inner-product) kernels: the centre is the box's, the scale covers
@@ -277,11 +297,10 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     } else if (kt == KS_LAPLACE) {
       rho = 0x1p-10f;                         // coincident points and near-cancellation
       t_flag = (float)(fabs(powe) * delta / tau);
-      // (c0 / d2)^m stays below 2^120 for d2 above c0 2^(-120/m)
+      // K stays below 2^120 for d2 above c0 2^(-120/m), c0 = scal^(1/m)
       const double mm = -powe, c0 = pow(scal, 1.0 / mm);
-      P->c0h = (float)c0;
-      P->c0l = (float)(c0 - (double)P->c0h);
       t_flag = fmaxf(t_flag, (float)(c0 * exp2(-120.0 / mm) * 1.001));
+      P->lap = lap_param(scal, powe);
     } else if (dist) {
       rho = 0.0f;                             // compact / polynomial in d2: absolute error only
     }
@@ -306,7 +325,7 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   const double delta = P->delta;
   TaskParam T;
   T.kp = kp;
-  T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.c0h = T.c0l = 0.0f;
+  T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.lap = LapParam{0, 0, 0.f, 0.f};
   T.centred = kt_uses_norms(kp.type) ? 1 : 0;
   if (kp.type == KS_GAUSSIAN) {
     const double s2 = kp.scal * 1.4426950408889634;
@@ -320,9 +339,8 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
     T.rho = 0x1p-10f;
     T.t_flag = (float)(fabs(kp.powe) * delta / tau);
     const double mm = -kp.powe, c0 = pow(kp.scal, 1.0 / mm);
-    T.c0h = (float)c0;
-    T.c0l = (float)(c0 - (double)T.c0h);
     T.t_flag = fmaxf(T.t_flag, (float)(c0 * exp2(-120.0 / mm) * 1.001));
+    T.lap = lap_param(kp.scal, kp.powe);
   }
   T.any_flag = (T.t_flag > 0.0f || T.rho > 0.0f) ? 1 : 0;
   out[t] = T;
@@ -486,32 +504,46 @@ struct SplitSmem {
   int abort;
   int never;             // stays 0: an abort flag for the drain waits
   double rsum[2][EPI_GROUPS - 1][BM];   // row sums of epilogue groups 1.., by item parity
+  float4 ltab[LTAB];     // Laplace log2 table
 };
 
-// Double-float (unevaluated FP32 pair) product, a *= b: Dekker's product with
-// the FMA giving the exact error of the high product.
-__device__ __forceinline__ void df_mul(float &ah, float &al, float bh, float bl)
+// Laplace table: for i in [0, 256), c_i ~ 1 / (1 + (i + 1/2) / 256) with 12
+// significant bits (so that r = f c_i - 1 is exact up to one rounding of a
+// value below 2^-8.8), and -log2(c_i) as an integer on the 2^-12 grid (bits in
+// .z) plus an FP32 remainder (.y).  Filled once per CTA in FP64.
+__device__ void laplace_table(float4 *tab)
 {
-  const float p = ah * bh;
-  float e = fmaf(ah, bh, -p);
-  e = fmaf(ah, bl, e);
-  e = fmaf(al, bh, e);
-  const float s = p + e;
-  al = e - (s - p);
-  ah = s;
+  for (int i = threadIdx.x; i < LTAB; i += blockDim.x) {
+    const double fm = 1.0 + (i + 0.5) / LTAB;
+    const double c = rint(4096.0 / fm) / 4096.0;
+    const double T = -log2(c);
+    const double th = rint(T * 4096.0);
+    tab[i] = make_float4((float)c, (float)(T - th / 4096.0), __int_as_float((int)th), 0.f);
+  }
 }
 
-// Double-float reciprocal, a = 1 / a, one Newton step on the FP32 quotient.
-__device__ __forceinline__ void df_rcp(float &ah, float &al)
+// scal * d2^powe for the double-float d2 = t + lo, powe = -P/2, as
+// 2^(log2 scal + powe log2 d2).  log2 d2 = e + (-log2 c_i) + log2(1 + r) +
+// lo / (t ln2) with t = 2^e f, i the top 8 bits of f and r = f c_i - 1; the
+// series of log2(1 + r) to r^4 (|r| < 2^-8.8).  The exponent's integer and
+// 2^-13-grid parts are formed exactly in int32, the rest in FP32, so that the
+// result carries a relative error of a few 1e-7 for every P up to 1022.
+// Values below 2^-126 flush to zero (rows of such values are redone in FP64).
+__device__ __forceinline__ float laplace_val(float t, float lo, const float4 *__restrict__ tab, const LapParam &L)
 {
-  float q = rcp_approx(ah);
-  q = fmaf(q, fmaf(-ah, q, 1.0f), q);        // Newton step: q to ~1 ulp of 1/ah
-  float r = fmaf(-ah, q, 1.0f);
-  r = fmaf(-al, q, r);
-  const float ql = q * r;
-  const float s = q + ql;
-  al = ql - (s - q);
-  ah = s;
+  const uint32_t u = __float_as_uint(t);
+  const int e = (int)(u >> 23) - 127;
+  const float4 tb = tab[(u >> 15) & (LTAB - 1)];
+  const float f = __uint_as_float((u & 0x007fffffu) | 0x3f800000u);
+  const float r = fmaf(f, tb.x, -1.0f);
+  const float p = r * fmaf(r, fmaf(r, fmaf(r, -0.36067376f, 0.48089835f), -0.72134752f), 1.44269504f);
+  const float llo = (tb.y + p) + lo * rcp_approx(t) * 1.44269504f;
+  const int lhi = e * 4096 + __float_as_int(tb.z);          // log2 d2 on the 2^-12 grid
+  const int E = L.ls13 - L.P * lhi;                          // 2^-13 units
+  const float arg = fmaf((float)(E & 8191), 0x1p-13f, fmaf(L.mh, llo, L.lsf));
+  const float y = ex2_approx(arg);
+  const int n = E >> 13;
+  return n >= -126 ? y * __int_as_float((n + 127) << 23) : 0.0f;
 }
 
 // 2^((t + lo)(ph + pl)) for a double-float distance and a double-float factor
@@ -555,28 +587,6 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
       return kp.pint < 0 ? 1.0f / r : r;
     }
     return ex2_approx((float)kp.powe * __log2f(v));
-  } else if constexpr (KT == KS_LAPLACE) {
-    // scal * d2^powe with powe = -m < 0 (k >= 3), evaluated as (c0 / d2)^m with
-    // c0 = scal^(1/m): the intermediates stay in the FP32 range for every d2
-    // whose kernel value does (smaller d2 are flagged and done in FP64).  The
-    // base is a double-float through binary powering: m up to 32 would
-    // amplify a single FP32 rounding of d2 m-fold.  hrow / hcol carry c0.
-    float bh = t, bl = lo;
-    df_rcp(bh, bl);
-    df_mul(bh, bl, hrow, hcol);
-    const int m = -kp.pint - (kp.pmode == POW_HALF ? 1 : 0);   // integer part of -powe
-    float rh = 1.0f, rl = 0.0f, ph = bh, pl = bl;
-#pragma unroll
-    for (int bit = 0; bit < 9; bit++) {      // fixed trip count (m < 512), uniform branches
-      if (m & (1 << bit)) df_mul(rh, rl, ph, pl);
-      if (m >> (bit + 1)) df_mul(ph, pl, ph, pl);
-    }
-    if (kp.pmode == POW_HALF) {
-      const float sh = sqrtf(bh);
-      const float sl = (fmaf(-sh, sh, bh) + bl) / (2.0f * sh);   // sqrt(bh + bl) = sh + sl
-      df_mul(rh, rl, sh, sl);
-    }
-    return rh + rl;
   } else if constexpr (KT == KS_TANH) {
     const float v = fmaf((float)kp.scal, c, (float)kp.cons);
     const float av = fabsf(v);
@@ -681,7 +691,8 @@ __device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const u
 template <int KT, bool EXACT, bool FLAGS, int NC>
 __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                               const PtMeta *__restrict__ bm, const PtMeta &am, float rc,
-                                              const TaskParam &T, float (&acc)[4])
+                                              const TaskParam &T, const float4 *__restrict__ ltab,
+                                              float (&acc)[4])
 {
   const KParams &kp = T.kp;
   uint32_t flags = 0;
@@ -693,7 +704,7 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
     float t, lo, s;
     assemble<EXACT>(__uint_as_float(h[j]), __uint_as_float(l[j]), am.n_hi, am.n_lo, m0.x, m0.y, rc, t, lo, s);
     float kv;
-    if constexpr (KT == KS_LAPLACE) kv = kval32<KT>(t, lo, 0.f, T.c0h, T.c0l, kp);
+    if constexpr (KT == KS_LAPLACE) kv = laplace_val(t, lo, ltab, T.lap);
     else if constexpr (KT == KS_GAUSS_UNSCALED) kv = exp2_prod(t, lo, T.s2, T.s2l);
     else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
       // factor h_i h_j (negative) as a float pair
@@ -754,9 +765,11 @@ __device__ void dump_chunk(float *dump, int row, int c0, const uint32_t (&h)[NC]
   }
 }
 
-__host__ __device__ constexpr bool kt_exponential(int kt)
+// Kernels whose FP32 values may fall below the FP32 range while FP64 keeps
+// them (the row rescue of tile_epilogue).
+__host__ __device__ constexpr bool kt_rescue(int kt)
 {
-  return kt == KS_GAUSSIAN || kt == KS_GAUSS_UNSCALED || kt == KS_GAUSSIAN_VAR_BANDWIDTH;
+  return kt == KS_GAUSSIAN || kt == KS_GAUSS_UNSCALED || kt == KS_GAUSSIAN_VAR_BANDWIDTH || kt == KS_LAPLACE;
 }
 
 // One warp's share of one tile (32 columns of its 32 rows): TMEM loads, kernel
@@ -767,7 +780,7 @@ __host__ __device__ constexpr bool kt_exponential(int kt)
 template <int KT>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
                                               const PtMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
-                                              bool gfast, bool dump, double &racc)
+                                              bool gfast, bool dump, const float4 *ltab, double &racc)
 {
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   double rchk = 0.0;
@@ -788,11 +801,11 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
       uint32_t flags = 0;
       const bool fl = T.any_flag != 0;
       if (exact) {
-        if (fl) flags = epi_chunk<KT, true, true, 16>(h, l, bm + c0, am, rc, T, acc);
-        else epi_chunk<KT, true, false, 16>(h, l, bm + c0, am, rc, T, acc);
+        if (fl) flags = epi_chunk<KT, true, true, 16>(h, l, bm + c0, am, rc, T, ltab, acc);
+        else epi_chunk<KT, true, false, 16>(h, l, bm + c0, am, rc, T, ltab, acc);
       } else {
-        if (fl) flags = epi_chunk<KT, false, true, 16>(h, l, bm + c0, am, rc, T, acc);
-        else epi_chunk<KT, false, false, 16>(h, l, bm + c0, am, rc, T, acc);
+        if (fl) flags = epi_chunk<KT, false, true, 16>(h, l, bm + c0, am, rc, T, ltab, acc);
+        else epi_chunk<KT, false, false, 16>(h, l, bm + c0, am, rc, T, ltab, acc);
       }
       // FP64 rechecks of the flagged pairs of these 16 columns
       while (flags) {
@@ -811,7 +824,7 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     }
   }
   const float fs = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-  if constexpr (kt_exponential(KT)) {
+  if constexpr (kt_rescue(KT)) {
     // A row whose kernel values over these 32 columns all lie below 2^-96
     // (FP32 flushes values below 2^-126 to zero, FP64 keeps them down to
     // 2^-1074) takes these pairs from FP64 instead, flagged pairs included.
@@ -864,6 +877,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     fence_mbar_init();
   }
   if (warp == 0) { tmem_alloc(&S->tmem_base, TMEM_COLS); tmem_relinquish(); }
+  if constexpr (KT == KS_LAPLACE || KT == KS_LIST) laplace_table(S->ltab);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -986,7 +1000,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     TaskParam T0;                                  // the single call's parameters
     if constexpr (KT != KS_LIST) {
       T0.kp = a.kp; T0.t_flag = P->t_flag; T0.rho = P->rho; T0.s2 = T0.s2l = 0.f;
-      T0.c0h = P->c0h; T0.c0l = P->c0l; T0.any_flag = P->any_flag; T0.centred = P->centred;
+      T0.lap = P->lap; T0.any_flag = P->any_flag; T0.centred = P->centred;
     }
     int g = 0, tc = 0;
     for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
@@ -1012,24 +1026,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         if constexpr (KT == KS_LIST) {
           switch (T.kp.type) {
             case KS_GAUSSIAN:
-              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
+              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
             case KS_POLYNOMIAL:
-              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
+              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
+              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
             case KS_TANH:
-              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
+              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
             case KS_QUARTIC:
-              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
+              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
             case KS_MULTIQUADRATIC:
-              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
+              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
             default:
-              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, racc); break;
+              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
           }
         } else {
-          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, racc);
+          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, S->ltab, racc);
         }
         tc_fence_before();
         __syncwarp();
