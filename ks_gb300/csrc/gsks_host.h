@@ -83,4 +83,14 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
                        const double *XB, const int *b_idx, int nxb, const double *w, const int *w_idx,
                        double *partial, cudaStream_t s, int *launches);
 
+// Owner lists of the batched merge (gsks_sort.cu): u_idx holds na device
+// indices in [0, nu) (others raise DEVERR_MAP_RANGE in *err).  Writes own_pos
+// (na: the positions grouped by u entry, ascending within an entry), ent_u
+// (the distinct entries, ascending), own_off (entry e owns own_pos[own_off[e]
+// .. own_off[e+1])) and *nent, all on the device; work holds
+// owner_work_bytes(na) bytes.
+size_t owner_work_bytes(int na);
+int owner_lists(const int *u_idx, int na, int nu, void *work, int *own_pos, int *ent_u, int *own_off, int *nent,
+                int *err, cudaStream_t s, int *launches);
+
 }  // namespace gsks

@@ -75,13 +75,13 @@ list_fp64_kernel(FusedArgs a, const KParams *__restrict__ kps, int per_task,
 
 // For each distinct u entry e: u[ent_u[e]] += sum over the list positions that
 // name it (ascending) of the sum over that position's source chunks.
-__global__ void list_merge(int nent, const int *__restrict__ ent_u, const int *__restrict__ own_off,
-                           const int *__restrict__ own_pos, int ntask, const int *__restrict__ a_off,
-                           const ListTask *__restrict__ tasks, const double *__restrict__ partial,
-                           double *__restrict__ u)
+__global__ void list_merge(const int *__restrict__ nent, const int *__restrict__ ent_u,
+                           const int *__restrict__ own_off, const int *__restrict__ own_pos, int ntask,
+                           const int *__restrict__ a_off, const ListTask *__restrict__ tasks,
+                           const double *__restrict__ partial, double *__restrict__ u)
 {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nent) return;
+  if (e >= *nent) return;
   double s = 0.0;
   for (int q = own_off[e]; q < own_off[e + 1]; q++) {
     const int pos = own_pos[q];
@@ -99,6 +99,15 @@ __global__ void list_merge(int nent, const int *__restrict__ ent_u, const int *_
   u[ent_u[e]] += s;
 }
 
+// Flags DEVERR_MAP_RANGE if an index lies outside [0, lim).
+__global__ void check_range(int n, const int *__restrict__ idx, int lim, int *err)
+{
+  bool bad = false;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += blockDim.x * gridDim.x)
+    bad |= (idx[i] < 0 || idx[i] >= lim);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, DEVERR_MAP_RANGE);
+}
+
 template <typename T>
 bool upload(DevBuf &b, const T *src, size_t n, cudaStream_t s)
 {
@@ -108,13 +117,13 @@ bool upload(DevBuf &b, const T *src, size_t n, cudaStream_t s)
 
 // Device-side state of the list path, per host thread.
 struct ListBufs {
-  DevBuf items, tasks, kps, counter, partial, ent_u, own_off, own_pos;
+  DevBuf items, tasks, kps, counter, partial, ent_u, own_off, own_pos, sort_work;
   DevBuf a_off, a_idx, b_idx, w_idx, u_idx;
   DevBuf XA, XB, XA2, XB2, w, u;
   std::vector<DevBuf> bandwidths;
   ~ListBufs()
   {
-    for (DevBuf *b : {&items, &tasks, &kps, &counter, &partial, &ent_u, &own_off, &own_pos, &a_off,
+    for (DevBuf *b : {&items, &tasks, &kps, &counter, &partial, &ent_u, &own_off, &own_pos, &sort_work, &a_off,
                       &a_idx, &b_idx, &w_idx, &u_idx, &XA, &XB, &XA2, &XB2, &w, &u})
       b->release();
     for (auto &b : bandwidths) b.release();
@@ -172,23 +181,6 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
       return set_status(GSKS_ERR_LIST, "dgsks_list");
   const int na = hoff_a[ntask], nb = hoff_b[ntask];
 
-  std::vector<int> hu_idx(na);
-  std::vector<int> tmp;
-  if (dev) {
-    if (na && cudaMemcpy(hu_idx.data(), u_idx, na * sizeof(int), cudaMemcpyDeviceToHost))
-      return cuda_status(cudaGetLastError(), "dgsks_list u_idx");
-  } else {
-    memcpy(hu_idx.data(), u_idx, na * sizeof(int));
-    auto bad = [](const int *v, int n, int lim) {
-      for (int i = 0; i < n; i++) if (v[i] < 0 || v[i] >= lim) return true;
-      return false;
-    };
-    if (bad(a_idx, na, nxa) || bad(b_idx, nb, nxb) || bad(w_idx, nb, nw))
-      return set_status(GSKS_ERR_MAP_RANGE, "dgsks_list");
-  }
-  for (int i = 0; i < na; i++)
-    if (hu_idx[i] < 0 || hu_idx[i] >= nu) return set_status(GSKS_ERR_MAP_RANGE, "dgsks_list");
-
   // ---- kernel descriptors -------------------------------------------------
   for (auto &b : L.bandwidths) b.release();
   L.bandwidths.clear();
@@ -228,6 +220,7 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
     const int m = hoff_a[t + 1] - hoff_a[t], n = hoff_b[t + 1] - hoff_b[t];
     const int nsc = (m > 0 && n > 0) ? (n + LIST_CHUNK - 1) / LIST_CHUNK : 0;
     tasks[t] = ListTask{pbase, m, nsc};
+    if (split) { pbase += (long long)nsc * m; continue; }   // the split form plans its own items
     for (int sc = 0; sc < nsc; sc++)
       for (int i0 = 0; i0 < m; i0 += fp64cfg::BM) {
         ListItem it{};
@@ -242,39 +235,37 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
     return (long long)x.rows * x.cols > (long long)y.rows * y.cols;
   });
 
-  // ---- owners of each u entry (counting sort by u index) ------------------
-  std::vector<int> cnt(nu + 1, 0);
-  for (int i = 0; i < na; i++) cnt[hu_idx[i] + 1]++;
-  std::vector<int> ent_u, own_off;
-  ent_u.reserve(std::min(nu, na)); own_off.reserve(std::min(nu, na) + 1);
-  std::vector<int> start(nu, 0);
-  int acc = 0;
-  for (int e = 0; e < nu; e++) {
-    if (cnt[e + 1]) { ent_u.push_back(e); own_off.push_back(acc); }
-    start[e] = acc;
-    acc += cnt[e + 1];
-  }
-  own_off.push_back(acc);
-  std::vector<int> own_pos(na);
-  for (int i = 0; i < na; i++) own_pos[start[hu_idx[i]]++] = i;  // ascending within an entry
-
   // ---- device data --------------------------------------------------------
   const double *dXA = XA, *dXB = XB, *dXA2 = nullptr, *dXB2 = nullptr, *dw = w;
   double *du = u;
-  const int *da_idx = a_idx, *db_idx = b_idx, *dw_idx = w_idx;
+  const int *da_idx = a_idx, *db_idx = b_idx, *dw_idx = w_idx, *du_idx = u_idx;
   bool ok = true;
   if (!dev) {
     ok = upload(L.XA, XA, (size_t)nxa * k, s) && upload(L.w, w, (size_t)nw, s) &&
          upload(L.u, u, (size_t)nu, s) && upload(L.a_idx, a_idx, (size_t)na, s) &&
-         upload(L.b_idx, b_idx, (size_t)nb, s) && upload(L.w_idx, w_idx, (size_t)nb, s);
+         upload(L.b_idx, b_idx, (size_t)nb, s) && upload(L.w_idx, w_idx, (size_t)nb, s) &&
+         (u_idx == a_idx || upload(L.u_idx, u_idx, (size_t)na, s));
     dXA = (const double *)L.XA.p;
     if (ok && XB != XA) { ok = upload(L.XB, XB, (size_t)nxb * k, s); dXB = (const double *)L.XB.p; }
     else dXB = dXA;
     dw = (const double *)L.w.p; du = (double *)L.u.p;
+    du_idx = u_idx == a_idx ? (const int *)L.a_idx.p : (const int *)L.u_idx.p;
     da_idx = (const int *)L.a_idx.p; db_idx = (const int *)L.b_idx.p; dw_idx = (const int *)L.w_idx.p;
   }
   if (!ok) return set_status(GSKS_ERR_ALLOC, "dgsks_list upload");
   int launches = 0;
+  // ---- index ranges, checked on the device before any kernel reads through them
+  {
+    int *err = (int *)c->err.p;
+    auto chk = [&](const int *idx, int n, int lim) {
+      if (n > 0) {
+        check_range<<<std::min((n + 255) / 256, 4096), 256, 0, s>>>(n, idx, lim, err);
+        launches++;
+      }
+    };
+    chk(da_idx, na, nxa); chk(db_idx, nb, nxb); chk(dw_idx, nb, nw); chk(du_idx, na, nu);
+    if (read_device_errors(c) & DEVERR_MAP_RANGE) return set_status(GSKS_ERR_MAP_RANGE, "dgsks_list");
+  }
   if (any_norms && !split) {   // the split form forms its own norms
     // caller-supplied norms are used as given; missing ones are computed on
     // the device (the list wrappers of frame/omp_dgsks_list.cpp:74-92)
@@ -300,11 +291,18 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
     }
   }
   ok = (split || upload(L.items, items.data(), items.size(), s)) && upload(L.tasks, tasks.data(), tasks.size(), s) &&
-       upload(L.kps, kps.data(), kps.size(), s) && upload(L.ent_u, ent_u.data(), ent_u.size(), s) &&
-       upload(L.own_off, own_off.data(), own_off.size(), s) &&
-       upload(L.own_pos, own_pos.data(), own_pos.size(), s) &&
-       L.partial.ensure(std::max<long long>(pbase, 1) * sizeof(double)) && L.counter.ensure(sizeof(int));
+       upload(L.kps, kps.data(), kps.size(), s) &&
+       L.partial.ensure(std::max<long long>(pbase, 1) * sizeof(double)) && L.counter.ensure(2 * sizeof(int)) &&
+       L.own_pos.ensure(std::max(na, 1) * sizeof(int)) && L.ent_u.ensure(std::max(na, 1) * sizeof(int)) &&
+       L.own_off.ensure((std::max(na, 1) + 1) * sizeof(int)) && L.sort_work.ensure(owner_work_bytes(na));
   if (!ok) return set_status(GSKS_ERR_ALLOC, "dgsks_list plan");
+  // owners of each u entry, ascending positions (device radix sort)
+  int *d_nent = (int *)L.counter.p + 1;
+  if (na > 0) {
+    const int st = owner_lists(du_idx, na, nu, L.sort_work.p, (int *)L.own_pos.p, (int *)L.ent_u.p,
+                               (int *)L.own_off.p, d_nent, (int *)c->err.p, s, &launches);
+    if (st) return set_status(st, "dgsks_list owners");
+  }
   if (!upload(L.a_off, hoff_a.data(), (size_t)ntask + 1, s)) return set_status(GSKS_ERR_ALLOC, "dgsks_list");
   const int *da_off = (const int *)L.a_off.p;
 
@@ -327,10 +325,10 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
                                                   (int *)L.counter.p, (double *)L.partial.p);
     launches++;
   }
-  if (!ent_u.empty()) {
-    list_merge<<<((int)ent_u.size() + 127) / 128, 128, 0, s>>>(
-        (int)ent_u.size(), (const int *)L.ent_u.p, (const int *)L.own_off.p, (const int *)L.own_pos.p,
-        ntask, da_off, (const ListTask *)L.tasks.p, (const double *)L.partial.p, du);
+  if (na > 0) {
+    list_merge<<<(na + 127) / 128, 128, 0, s>>>(d_nent, (const int *)L.ent_u.p, (const int *)L.own_off.p,
+                                                (const int *)L.own_pos.p, ntask, da_off,
+                                                (const ListTask *)L.tasks.p, (const double *)L.partial.p, du);
     launches++;
   }
   cudaError_t e = cudaGetLastError();

@@ -104,7 +104,9 @@ constexpr int KS_LIST = 99;
 constexpr int KS_GAUSS_UNSCALED = 100;
 
 // Epilogue parameters of one task (a single call uses one, built from Params).
-struct TaskParam {
+// The list form copies each item's entry into shared memory with the target
+// tile (a bulk copy: 16-byte multiple).
+struct __align__(16) TaskParam {
   KParams kp;
   float t_flag, rho;     // flag pairs with t < t_flag or t < rho * (n_i + n_j)
   float s2, s2l;         // Gaussian of the list form: scal * log2(e) = s2 + s2l
@@ -112,6 +114,7 @@ struct TaskParam {
   int any_flag;
   int centred;           // distance kernels: coordinates taken relative to the centre
 };
+static_assert(sizeof(TaskParam) % 16 == 0, "TaskParam is copied by the bulk-copy engine");
 
 // One work item of the list form: a target tile and a range of source tiles of
 // one task; the rows' partial sums go to partial[out + row].
@@ -197,7 +200,10 @@ __device__ __forceinline__ int pool_index(const int *map, int pos, int npool, in
   return p;
 }
 
-// Per-dimension min / max over the gathered targets and sources.
+// Per-dimension min / max over the gathered targets and sources.  Every thread
+// keeps one dimension (the grid-wide thread count is rounded down to a
+// multiple of k; at least k threads are launched) and folds its points in
+// registers; one shared and one global atomic per thread and bound.
 __global__ void bbox_kernel(int m, int n, int k, const double *__restrict__ XA, const int *__restrict__ amap,
                             int nxa, const double *__restrict__ XB, const int *__restrict__ bmap, int nxb,
                             int *err, long long *bbox)
@@ -208,16 +214,22 @@ __global__ void bbox_kernel(int m, int n, int k, const double *__restrict__ XA, 
     sb[k + p] = (long long)0x8000000000000000ULL;
   }
   __syncthreads();
-  const long long total = (long long)(m + n) * k;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)blockDim.x * gridDim.x) {
-    const int pt = (int)(e / k), p = (int)(e - (long long)pt * k);
-    double v;
-    if (pt < m) v = XA[(size_t)pool_index(amap, pt, nxa, err) * k + p];
-    else v = XB[(size_t)pool_index(bmap, pt - m, nxb, err) * k + p];
-    const long long key = dkey(v);
-    atomicMin(&sb[p], key);
-    atomicMax(&sb[k + p], key);
+  const long long nthr = (long long)blockDim.x * gridDim.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long per = nthr / k;                      // points advanced per step
+  if (tid < per * k) {
+    const int p = (int)(tid % k);
+    long long lo = 0x7FFFFFFFFFFFFFFFLL, hi = (long long)0x8000000000000000ULL;
+    for (long long pt = tid / k; pt < (long long)m + n; pt += per) {
+      double v;
+      if (pt < m) v = XA[(size_t)pool_index(amap, (int)pt, nxa, err) * k + p];
+      else v = XB[(size_t)pool_index(bmap, (int)(pt - m), nxb, err) * k + p];
+      const long long key = dkey(v);
+      lo = min(lo, key);
+      hi = max(hi, key);
+    }
+    atomicMin(&sb[p], lo);
+    atomicMax(&sb[k + p], hi);
   }
   __syncthreads();
   for (int p = threadIdx.x; p < k; p += blockDim.x) {
@@ -505,7 +517,15 @@ struct SplitSmem {
   int never;             // stays 0: an abort flag for the drain waits
   double rsum[2][EPI_GROUPS - 1][BM];   // row sums of epilogue groups 1.., by item parity
   float4 ltab[LTAB];     // Laplace log2 table
+  TaskParam tslot[2];    // list form: the current items' task parameters, by item parity
 };
+
+template <int KT>
+__device__ __forceinline__ const TaskParam &pick_task(const TaskParam &slot, const TaskParam &single)
+{
+  if constexpr (KT == KS_LIST) return slot;
+  else return single;
+}
 
 // Laplace table: for i in [0, 256), c_i ~ 1 / (1 + (i + 1/2) / 256) with 12
 // significant bits (so that r = f c_i - 1 is exact up to one rounding of a
@@ -899,13 +919,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         const ItemGeo G = item_geo(a, item);
         if (it > 0 && !mbar_wait(&S->a_empty, (it - 1) & 1, abort, WAIT_LIMIT)) break;
         const uint8_t *imgA = a.imgA + (size_t)G.ti * a_bytes;
+        // slot it & 1 was last read for item it - 2, which every epilogue warp
+        // has finished once it arrived on a_empty for item it - 1
+        const uint32_t tp_bytes = a.tab ? (uint32_t)sizeof(TaskParam) : 0u;
         if (resident) {
-          mbar_arrive_expect_tx(&S->a_full, (uint32_t)a_bytes);
+          mbar_arrive_expect_tx(&S->a_full, (uint32_t)a_bytes + tp_bytes);
           bulk_g2s(sA, imgA, (uint32_t)a_bytes, &S->a_full);
         } else {
-          mbar_arrive_expect_tx(&S->a_full, (uint32_t)meta_bytes);
+          mbar_arrive_expect_tx(&S->a_full, (uint32_t)meta_bytes + tp_bytes);
           bulk_g2s(sAmeta, imgA + a_op, (uint32_t)meta_bytes, &S->a_full);
         }
+        if (tp_bytes) bulk_g2s(&S->tslot[it & 1], a.tp + G.task, tp_bytes, &S->a_full);
         a_issued = it;
         for (int tj = G.t0; tj < G.t1 && !stop; tj++, tt++) {
           const uint8_t *imgB = a.imgB + (size_t)tj * b_bytes;
@@ -1005,10 +1029,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     int g = 0, tc = 0;
     for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
       const ItemGeo G = item_geo(a, item);
-      TaskParam T;
-      if constexpr (KT == KS_LIST) T = a.tp[G.task];
-      else T = T0;
       if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
+      const TaskParam &T = pick_task<KT>(S->tslot[it & 1], T0);
       const PtMeta am = ((const PtMeta *)sAmeta)[row];
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->a_empty);
@@ -1169,7 +1191,8 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   bbox_init<<<1, 256, 0, s>>>(k, bbox);
   {
     const long long tot = (long long)(m + n) * k;
-    const int blocks = (int)std::min<long long>(4LL * sms, std::max<long long>(1, (tot + 255) / 256));
+    const int blocks = (int)std::max<long long>((k + 255) / 256,
+                                                std::min<long long>(4LL * sms, std::max<long long>(1, (tot + 255) / 256)));
     bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(m, n, k, XA, amap, nxa, XB, bmap, nxb,
                                                                (int *)c->err.p, bbox);
   }
@@ -1311,7 +1334,8 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
     // every list position (tasks with an empty side included: harmless)
     const int ma = hoff_a[ntask], mb = hoff_b[ntask];
     const long long tot = ((long long)ma + mb) * k;
-    const int blocks = (int)std::min<long long>(4LL * sms, std::max<long long>(1, (tot + 255) / 256));
+    const int blocks = (int)std::max<long long>((k + 255) / 256,
+                                                std::min<long long>(4LL * sms, std::max<long long>(1, (tot + 255) / 256)));
     bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(ma, mb, k, XA, a_idx, nxa, XB, b_idx, nxb, err, bbox);
   }
   params_kernel<<<1, 1024, 0, s>>>(k, KS_LIST, 0.0, 0.0, tau, bbox, centre, P);
