@@ -220,6 +220,7 @@ __global__ void bbox_kernel(int m, int n, int k, const double *__restrict__ XA, 
   if (tid < per * k) {
     const int p = (int)(tid % k);
     long long lo = 0x7FFFFFFFFFFFFFFFLL, hi = (long long)0x8000000000000000ULL;
+#pragma unroll 4
     for (long long pt = tid / k; pt < (long long)m + n; pt += per) {
       double v;
       if (pt < m) v = XA[(size_t)pool_index(amap, (int)pt, nxa, err) * k + p];
@@ -324,6 +325,7 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     P->exact_t1 = (q <= 2.0 * sigma * sigma * 0x1p-14) ? 1 : 0;
     P->gfast = (kt == KS_GAUSSIAN && P->exact_t1 && !P->any_flag) ? 1 : 0;
   }
+
 }
 
 // Per-task epilogue parameters of the list form (coordinates unscaled, alpha = 1):
@@ -385,32 +387,37 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   }
   const int pidx = valid ? pool_index(map, pt, npool, err) : 0;
   const double *x = X + (size_t)pidx * k;
-  const double alpha = P->alpha, inv_sigma = P->inv_sigma;
+  const double sc = P->alpha * P->inv_sigma * 128.0;        // coordinate -> slice units
   uint8_t *base = img + (size_t)tile * tile_bytes(BM, kpad);
   const size_t bb = blk_bytes(BM, kpad);
-  double nrm = 0.0;
+  // The norm of the represented point restricted to the products the tensor
+  // cores form (a1a1 + 2a1a2 + a2a2 + 2a1a3), so that the assembled d2 of
+  // identical points is 0 up to the FP32 accumulations.  Every term is an
+  // integer multiple of 2^-48 (halves are multiples of 2^-24): summed exactly
+  // in integers, a1a1 at scale 1, 2a1(a2 + a3) at 2^24, a2a2 at 2^48.  FP64
+  // instructions issue slowly here; the slicing uses six per coordinate.
+  int n_i = 0;
+  long long n_a = 0, n_b = 0;
   for (int kg = 0; kg < kpad / 8; kg++) {
     __align__(16) __half s1[8], s2[8], s3[8];
 #pragma unroll
     for (int e = 0; e < 8; e++) {
       const int p = kg * 8 + e;
-      double a1 = 0.0, r1 = 0.0;
+      float a1 = 0.0f;
       __half h2 = __float2half_rn(0.0f), h3 = __float2half_rn(0.0f);
       if (valid && p < k) {
-        const double xv = alpha * (x[p] - (centred ? centre[p] : 0.0));
-        const double t = xv * inv_sigma * 128.0;
-        a1 = rint(t);
-        r1 = t - a1;                                   // |r1| <= 0.5, exact
-        h2 = __float2half_rn((float)r1);
-        const double r2 = r1 - (double)__half2float(h2);
-        h3 = __float2half_rn((float)r2);
-        // The norm of the represented point restricted to the products the
-        // tensor cores form (a1a1 + 2a1a2 + a2a2 + 2a1a3), so that the
-        // assembled d2 of identical points is 0 up to the FP32 accumulations.
-        const double f2 = (double)__half2float(h2), f3 = (double)__half2float(h3);
-        nrm += (a1 * a1 + 2.0 * a1 * f2 + f2 * f2 + 2.0 * a1 * f3) * (1.0 / 16384.0);
+        const double t = (centred ? x[p] - centre[p] : x[p]) * sc;   // the difference is exact near the centre
+        a1 = rintf((float)t);                          // |a1| <= 128
+        const float r1 = (float)(t - (double)a1);      // |r1| <= 1/2 (+ a rounding at ties)
+        h2 = __float2half_rn(r1);
+        h3 = __float2half_rn(r1 - __half2float(h2));   // the difference is exact in FP32
+        const int ia = (int)a1;
+        const int F2 = (int)(__half2float(h2) * 16777216.0f), F3 = (int)(__half2float(h3) * 16777216.0f);
+        n_i += ia * ia;
+        n_a += (long long)(2 * ia) * (F2 + F3);
+        n_b += (long long)F2 * F2;
       }
-      s1[e] = __float2half_rn((float)a1);              // exact: |a1| <= 128
+      s1[e] = __float2half_rn(a1);                     // exact
       s2[e] = h2;
       s3[e] = h3;
     }
@@ -418,6 +425,7 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
     *(uint4 *)(base + img_off(1, kg, r, kpad)) = *(const uint4 *)s2;
     *(uint4 *)(base + img_off(2, kg, r, kpad)) = *(const uint4 *)s3;
   }
+  const double nrm = ((double)n_i + (double)n_a * 0x1p-24 + (double)n_b * 0x1p-48) * (1.0 / 16384.0);
   (void)bb;
   // The norm in units of the accumulators: nu = |x''|^2 / g with
   // g = 2 sigma^2 2^-14, so that d2 = g (nu_i + nu_j - H - L).  nu is split on
@@ -1192,7 +1200,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   {
     const long long tot = (long long)(m + n) * k;
     const int blocks = (int)std::max<long long>((k + 255) / 256,
-                                                std::min<long long>(4LL * sms, std::max<long long>(1, (tot + 255) / 256)));
+                                                std::min<long long>(8LL * sms, std::max<long long>(1, (tot + 255) / 256)));
     bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(m, n, k, XA, amap, nxa, XB, bmap, nxb,
                                                                (int *)c->err.p, bbox);
   }
@@ -1335,7 +1343,7 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
     const int ma = hoff_a[ntask], mb = hoff_b[ntask];
     const long long tot = ((long long)ma + mb) * k;
     const int blocks = (int)std::max<long long>((k + 255) / 256,
-                                                std::min<long long>(4LL * sms, std::max<long long>(1, (tot + 255) / 256)));
+                                                std::min<long long>(8LL * sms, std::max<long long>(1, (tot + 255) / 256)));
     bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(ma, mb, k, XA, a_idx, nxa, XB, b_idx, nxb, err, bbox);
   }
   params_kernel<<<1, 1024, 0, s>>>(k, KS_LIST, 0.0, 0.0, tau, bbox, centre, P);
