@@ -82,6 +82,8 @@ struct PtMeta {          // 32 bytes per point, appended to each tile image
 struct LapParam {
   int P, ls13;
   float lsf, mh;         // mh = -P/2
+  float tover;           // d2 below tover: K may exceed the FP32 range
+  int pad[3];
 };
 
 struct Params {          // per call, computed on the device
@@ -94,6 +96,7 @@ struct Params {          // per call, computed on the device
   int any_flag;          // some pair may be flagged
   int exact_t1;          // nu_i + nu_j - H is exact in FP32
   int gfast;             // Gaussian without flags: low norm parts folded into w / row factors
+  int ff_ok;             // coordinates within 2^50: float-pair rechecks stay in range
   LapParam lap;          // Laplace exponent constants
   double delta;          // absolute error bound of the assembled d2 (scaled units)
 };
@@ -248,6 +251,9 @@ __device__ LapParam lap_param(double scal, double powe)
   L.ls13 = (int)l13;
   L.lsf = (float)(ls - l13 / 8192.0);
   L.mh = -0.5f * (float)L.P;
+  const double mm = -powe;
+  L.tover = (float)(pow(scal, 1.0 / mm) * exp2(-120.0 / mm) * 1.001);   // K = 2^120 at d2 = c0 2^(-120/m)
+  L.pad[0] = L.pad[1] = L.pad[2] = 0;
   return L;
 }
 
@@ -324,6 +330,7 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     // (it stays below 2^24 q), and only the small L term needs Fast2Sum.
     P->exact_t1 = (q <= 2.0 * sigma * sigma * 0x1p-14) ? 1 : 0;
     P->gfast = (kt == KS_GAUSSIAN && P->exact_t1 && !P->any_flag) ? 1 : 0;
+    P->ff_ok = (s_mx[0] <= 0x1p50) ? 1 : 0;
   }
 
 }
@@ -339,7 +346,7 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   const double delta = P->delta;
   TaskParam T;
   T.kp = kp;
-  T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.lap = LapParam{0, 0, 0.f, 0.f};
+  T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.lap = LapParam{0, 0, 0.f, 0.f, 0.f, {0, 0, 0}};
   T.centred = kt_uses_norms(kp.type) ? 1 : 0;
   if (kp.type == KS_GAUSSIAN) {
     const double s2 = kp.scal * 1.4426950408889634;
@@ -358,6 +365,16 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   }
   T.any_flag = (T.t_flag > 0.0f || T.rho > 0.0f) ? 1 : 0;
   out[t] = T;
+}
+
+// Float-pair copy of a pool: Xf[i] = (hi, lo), hi + lo = X[i] to 2^-48.
+__global__ void pool_split(long long n, const double *__restrict__ X, float2 *__restrict__ Xf)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)blockDim.x * gridDim.x) {
+    const double v = X[i];
+    const float h = (float)v;
+    Xf[i] = make_float2(h, (float)(v - (double)h));
+  }
 }
 
 // Tile images: per tile, NBLK slice blocks in the no-swizzle K-major core-matrix
@@ -473,6 +490,7 @@ struct TileArgs {
   int ntm, ntn, nsc, chunk_tiles;   // items = ntm * nsc; chunk = source tiles per item
   const uint8_t *imgA, *imgB;
   const double *XA, *XB;            // pool coordinates (FP64) for the rechecks
+  const float2 *XAf, *XBf;          // list form: the pools as float pairs (or nullptr)
   const int *amap, *bmap, *wmap;
   int nxa, nxb;                     // pool sizes for the map range checks (-1: unchecked)
   const double *w;
@@ -557,7 +575,8 @@ __device__ void laplace_table(float4 *tab)
 // 2^-13-grid parts are formed exactly in int32, the rest in FP32, so that the
 // result carries a relative error of a few 1e-7 for every P up to 1022.
 // Values below 2^-126 flush to zero (rows of such values are redone in FP64).
-__device__ __forceinline__ float laplace_val(float t, float lo, const float4 *__restrict__ tab, const LapParam &L)
+__device__ __forceinline__ float laplace_core(float t, float lo, const float4 *__restrict__ tab, const LapParam &L,
+                                              int &n)
 {
   const uint32_t u = __float_as_uint(t);
   const int e = (int)(u >> 23) - 127;
@@ -569,9 +588,22 @@ __device__ __forceinline__ float laplace_val(float t, float lo, const float4 *__
   const int lhi = e * 4096 + __float_as_int(tb.z);          // log2 d2 on the 2^-12 grid
   const int E = L.ls13 - L.P * lhi;                          // 2^-13 units
   const float arg = fmaf((float)(E & 8191), 0x1p-13f, fmaf(L.mh, llo, L.lsf));
-  const float y = ex2_approx(arg);
-  const int n = E >> 13;
+  n = E >> 13;
+  return ex2_approx(arg);
+}
+__device__ __forceinline__ float laplace_val(float t, float lo, const float4 *__restrict__ tab, const LapParam &L)
+{
+  int n;
+  const float y = laplace_core(t, lo, tab, L, n);
   return n >= -126 ? y * __int_as_float((n + 127) << 23) : 0.0f;
+}
+
+// 2^n y in FP64, n in the FP64 exponent range (beyond it, 0 or inf).
+__device__ __forceinline__ double scale2(float y, int n)
+{
+  if (n < -1022) return 0.0;
+  if (n > 1023) return (double)y * 0x1p1023 * 2.0;
+  return (double)y * __longlong_as_double((long long)(n + 1023) << 52);
 }
 
 // 2^((t + lo)(ph + pl)) for a double-float distance and a double-float factor
@@ -583,6 +615,19 @@ __device__ __forceinline__ float exp2_prod(float t, float lo, float ph, float pl
   const float ae = fmaf(t, ph, -a) + fmaf(lo, ph, t * pl);
   const float e = ex2_approx(a);
   return fmaf(e, 0.69314718f * ae, e);
+}
+
+// 2^((t + lo)(ph + pl)) as exp2_prod, returned in FP64 so that values below
+// the FP32 range keep their size (the integer part of the exponent is applied
+// in FP64).
+__device__ __forceinline__ double exp2_prod_wide(float t, float lo, float ph, float pl)
+{
+  const float a = t * ph;
+  const float ae = fmaf(t, ph, -a) + fmaf(lo, ph, t * pl);
+  const float n = floorf(a);
+  const float f = (a - n) + ae;                  // a - n is exact
+  const float e = ex2_approx(f);
+  return scale2(e, (int)n);
 }
 
 // FP32 kernel value from the double-float squared distance t + lo (scaled
@@ -643,12 +688,8 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
 // FP64 recheck of one flagged pair from the pool coordinates (the distance
 // assembly of near-coincident pairs is kept in FP64).
 template <int KT>
-__device__ double recheck64(const TileArgs &a, const KParams &kp, int ipos, int jpos)
+__device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb, int jpos)
 {
-  int pa = a.amap ? a.amap[ipos] : ipos;
-  int pb = a.bmap ? a.bmap[jpos] : jpos;
-  if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
-  if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
   const double *x = a.XA + (size_t)pa * a.k, *y = a.XB + (size_t)pb * a.k;
   double d2 = 0.0;
   for (int p = 0; p < a.k; p++) { const double d = x[p] - y[p]; d2 = fma(d, d, d2); }
@@ -665,6 +706,58 @@ __device__ double recheck64(const TileArgs &a, const KParams &kp, int ipos, int 
   else if constexpr (KT == KS_EPANECHNIKOV) kv = d2 < 1.0 ? 0.75 * (1.0 - d2) : 0.0;
   else kv = 0.0;
   return kv * wv;
+}
+
+// Recheck of one pair.  The list form keeps float-pair copies of the pools:
+// there the squared distance is summed in float-pair arithmetic (TwoSum per
+// coordinate difference, exact square by FMA; about 2^-44 relative) and the
+// kernel value is formed in FP32 from it, as in the main epilogue; FP64
+// instructions issue too slowly on this GPU to recheck many pairs.  Coincident
+// and overflowing Laplace pairs, the other kernels and the single-call form go
+// through FP64.
+template <int KT>
+__device__ double recheck(const TileArgs &a, const TaskParam &T, const float4 *ltab, int ipos, int jpos)
+{
+  int pa = a.amap ? a.amap[ipos] : ipos;
+  int pb = a.bmap ? a.bmap[jpos] : jpos;
+  if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
+  if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
+  if constexpr (KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH || KT == KS_LAPLACE) {
+    if (a.XAf && a.P->ff_ok) {
+      const float2 *x = a.XAf + (size_t)pa * a.k, *y = a.XBf + (size_t)pb * a.k;
+      float sh = 0.f, sl = 0.f;
+      for (int p = 0; p < a.k; p++) {
+        const float2 u = x[p], v = y[p];
+        const float s = u.x - v.x;                       // TwoSum(u.x, -v.x)
+        const float bv = s - u.x;
+        float e = (u.x - (s - bv)) + (-v.x - bv);
+        e += u.y - v.y;
+        const float dh = s + e, dl = e - (dh - s);       // Fast2Sum
+        const float q = dh * dh;
+        const float qe = fmaf(dh, dh, -q) + 2.f * dh * dl;
+        const float t = sh + q;                          // TwoSum(sh, q)
+        const float z = t - sh;
+        sl += ((sh - (t - z)) + (q - z)) + qe;
+        sh = t;
+      }
+      const float th = sh + sl, tl = sl - (th - sh);
+      const double wv = a.w[a.wmap ? a.wmap[jpos] : jpos];
+      if constexpr (KT == KS_GAUSS_UNSCALED) {
+        return exp2_prod_wide(th, tl, T.s2, T.s2l) * wv;
+      } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
+        const double f = -0.5 * 1.4426950408889634 * T.kp.hi[pa] * T.kp.hj[pb];
+        const float fh = (float)f, fl = (float)(f - (double)fh);
+        return exp2_prod_wide(th, tl, fh, fl) * wv;
+      } else {
+        if (th > T.lap.tover && th >= 1e-15f) {
+          int n;
+          const float y = laplace_core(th, tl, ltab, T.lap, n);
+          return scale2(y, n) * wv;
+        }
+      }
+    }
+  }
+  return recheck64<KT>(a, T.kp, pa, pb, jpos);
 }
 
 // Squared distance t + lo (double-float, scaled units) of one pair from its
@@ -841,7 +934,7 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
         flags &= flags - 1;
         const int c = c0 + j;
         if (c < ncols && am.pos >= 0) {
-          const double v = recheck64<KT>(a, T.kp, am.pos, bm[c].pos);
+          const double v = recheck<KT>(a, T, ltab, am.pos, bm[c].pos);
           rchk += v;
           fchk += fabsf((float)v);
           nchk = true;
@@ -860,7 +953,7 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W) {
       double r = 0.0;
       const int c1 = min(grp * 32 + 32, ncols);
-      for (int c = grp * 32; c < c1; c++) r += recheck64<KT>(a, T.kp, am.pos, bm[c].pos);
+      for (int c = grp * 32; c < c1; c++) r += recheck<KT>(a, T, ltab, am.pos, bm[c].pos);
       if constexpr (KT == KS_GAUSSIAN) {
         if (gfast) r /= (double)am.h;   // the caller applies the row factor to the row sum
       }
@@ -1317,7 +1410,11 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
   const size_t o_tp = o_kps + al((size_t)ntask * sizeof(KParams));
   const size_t o_a = o_tp + al((size_t)ntask * sizeof(TaskParam));
   const size_t o_b = o_a + al(ta.size() * tile_bytes(BM, kpad));
-  const size_t total = o_b + al(tb.size() * tile_bytes(BN, kpad));
+  // float-pair copies of the pools for the rechecks (one when both sides share it)
+  const bool same_pool = XA == XB && nxa == nxb;
+  const size_t o_xaf = o_b + al(tb.size() * tile_bytes(BN, kpad));
+  const size_t o_xbf = o_xaf + al((size_t)nxa * k * sizeof(float2));
+  const size_t total = o_xbf + (same_pool ? 0 : al((size_t)nxb * k * sizeof(float2)));
   if (!c->dwork.ensure(total)) return GSKS_ERR_ALLOC;
   uint8_t *ws = (uint8_t *)c->dwork.p;
   Params *P = (Params *)(ws + o_params);
@@ -1354,8 +1451,16 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
   pack_kernel<<<(int)tb.size(), BN, 0, s>>>(1, 0, k, kpad, XB, b_idx, nxb, err, w, w_idx, nullptr, KS_LIST,
                                             centre, P, ws + o_b, (const int2 *)(ws + o_tb),
                                             (const int *)(ws + o_tbt), tp);
+  float2 *xaf = (float2 *)(ws + o_xaf), *xbf = same_pool ? xaf : (float2 *)(ws + o_xbf);
+  {
+    const long long na_c = (long long)nxa * k, nb_c = (long long)nxb * k;
+    pool_split<<<(int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1), 256, 0, s>>>(na_c, XA, xaf);
+    if (!same_pool)
+      pool_split<<<(int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1), 256, 0, s>>>(nb_c, XB, xbf);
+  }
   TileArgs a{};
   a.k = k; a.kpad = kpad; a.kt = KS_LIST;
+  a.XAf = xaf; a.XBf = xbf;
   a.imgA = ws + o_a; a.imgB = ws + o_b;
   a.XA = XA; a.XB = XB; a.amap = a_idx; a.bmap = b_idx; a.wmap = w_idx; a.w = w;
   a.nxa = nxa; a.nxb = nxb;
