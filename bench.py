@@ -23,6 +23,10 @@ Reported (one JSON line):
   cpu_baseline  the oracle's port of the reference's fused dgsks on all host
              cores over sampled target rows x all sources; its row sums also
              give the errors of both forms (normwise and conditioned).
+  list       the batched configuration (20000 tasks over a 1M-point pool,
+             k = 16, mixed kernels) through dgsks_list in both forms, with
+             errors on a task subset and the oracle's OpenMP list driver as
+             CPU baseline (skipped with --no-list).
   --impl reference times that CPU implementation alone (the reference's own
   micro-kernels are AVX and do not build on the aarch64 host).
 
@@ -55,6 +59,12 @@ WORKLOAD = ("general stride: pool 262144 x k=64 uniform[0,1] FP64; m=n=65536 ran
             "u/w maps random permutations of [0,65536); Gaussian h=0.5 + Laplace + polynomial pwr=3")
 SPLIT_PRODUCTS = 6   # tensor-core products per slice pair set (a1b1, a1b2, a2b1, a2b2, a1b3, a3b1)
 
+# The batched configuration (dgsks_list), reported beside the headline.
+LIST_POOL, LIST_K, LIST_TASKS = 1 << 20, 16, 20000
+LIST_WORKLOAD = ("batched dgsks_list: 20000 independent (amap, bmap) pairs over a pool of 1,048,576 points in "
+                 "k=16 uniform[0,1]; list sizes log-uniform in [32, 4096]; kernel per task drawn from {Gaussian "
+                 "h~U[0.1,2], Laplace, polynomial pwr 2 or 3 (scal 1/k, cons 1)}; w ~ N(0,1)")
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -72,6 +82,7 @@ def parse():
     ap.add_argument("--m", type=int, default=M_T)
     ap.add_argument("--n", type=int, default=N_S)
     ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--no-list", action="store_true", help="skip the batched (dgsks_list) section")
     return ap.parse_args()
 
 
@@ -358,7 +369,153 @@ def run_ours(args, ws, rank, local):
         line["error"] = err
     if not args.no_e2e:
         line["e2e"] = run_e2e(args, torch, gsks, wl, ws, head)
+    if not args.no_list and ws == 1:
+        del wl
+        torch.cuda.empty_cache()
+        line["list"] = run_list(args, torch, gsks, forms)
     return line
+
+
+def make_list_workload(ntask=LIST_TASKS, seed=4321):
+    """Seeded synthetic lists: every task's targets (sources) are a window of a
+    random permutation of the pool, so they are distinct within the task."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    N = LIST_POOL
+
+    def lists(sz):
+        perm = rng.permutation(N).astype(np.int32)
+        off = np.concatenate([[0], np.cumsum(sz)]).astype(np.int64)
+        tid = np.repeat(np.arange(ntask), sz)
+        local = np.arange(off[-1]) - off[tid]
+        start = rng.integers(0, N, ntask)
+        return off.astype(np.int32), perm[(start[tid] + local) % N].astype(np.int32)
+
+    sa = np.exp(rng.uniform(np.log(32), np.log(4096), ntask)).astype(np.int64)
+    sb = np.exp(rng.uniform(np.log(32), np.log(4096), ntask)).astype(np.int64)
+    a_off, a_idx = lists(sa)
+    b_off, b_idx = lists(sb)
+    kinds = rng.integers(0, 3, ntask)
+    specs = []
+    for t in range(ntask):
+        if kinds[t] == 0:
+            specs.append((0, dict(scal=-1.0 / (2 * rng.uniform(0.1, 2.0) ** 2))))
+        elif kinds[t] == 1:
+            specs.append((2, {}))
+        else:
+            specs.append((1, dict(scal=1.0 / LIST_K, cons=1.0, powe=float(rng.integers(2, 4)))))
+    X = rng.random((N, LIST_K))
+    w = rng.standard_normal(N)
+    return dict(X=X, w=w, a_off=a_off, a_idx=a_idx, b_off=b_off, b_idx=b_idx, specs=specs,
+                sa=sa, sb=sb, pairs=float(np.sum(sa * sb)))
+
+
+def _sub_list(L, tasks):
+    import numpy as np
+    out = {}
+    for side in ("a", "b"):
+        off, idx = L[side + "_off"], L[side + "_idx"]
+        parts = [idx[off[t]:off[t + 1]] for t in tasks]
+        out[side + "_off"] = np.concatenate([[0], np.cumsum([p.size for p in parts])]).astype(np.int32)
+        out[side + "_idx"] = np.concatenate(parts).astype(np.int32)
+    out["specs"] = [L["specs"][t] for t in tasks]
+    out["pairs"] = float(sum(L["sa"][t] * L["sb"][t] for t in tasks))
+    return out
+
+
+def run_list(args, torch, gsks, forms):
+    """The batched configuration through dgsks_list with device arrays: wall
+    clock around each synchronous call (host planning included); errors of both
+    forms on a random subset of tasks against the oracle; the oracle's
+    multi-threaded restatement of the reference's list driver as CPU baseline."""
+    import numpy as np
+    from oracle import oracle as O
+    L = make_list_workload()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    X, w = dev(L["X"]), dev(L["w"])
+    out = {"workload": LIST_WORKLOAD, "tasks": LIST_TASKS, "pairs_per_step": L["pairs"],
+           "timing": "wall clock around each synchronous dgsks_list call, device-resident arrays; "
+                     "host planning, uploads of the plan and the merge included"}
+
+    def call(sub, u, kers):
+        gsks.dgsks_list(kers[0], u, dev(sub["a_off"]), dev(sub["a_idx"]), dev(sub["b_off"]), dev(sub["b_idx"]),
+                        X, None, X, None, w, kers=kers)
+
+    kers = [gsks.make_kernel(t, **p) for t, p in L["specs"]]
+    d_lists = {k: dev(L[k]) for k in ("a_off", "a_idx", "b_off", "b_idx")}
+    for form in forms:
+        gsks.set_precision(prec_of(gsks, form))
+        u = torch.zeros(LIST_POOL, dtype=torch.float64, device="cuda")
+        run = lambda: gsks.dgsks_list(kers[0], u, d_lists["a_off"], d_lists["a_idx"], d_lists["b_off"],
+                                      d_lists["b_idx"], X, None, X, None, w, kers=kers)
+        for _ in range(max(1, args.warmup)):
+            run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[form] = {"value": L["pairs"] * args.steps / dt, "unit": "pair-evals/s",
+                     "ms_per_step": dt * 1e3 / args.steps, "gpu_launches": gsks.last_launch_count()}
+    gsks.set_precision(gsks.GSKS_FP64)
+    if "split" in out and "fp64" in out:
+        out["split_over_fp64"] = out["split"]["value"] / out["fp64"]["value"]
+
+    # errors on a subset of tasks
+    rng = np.random.default_rng(17)
+    sub = _sub_list(L, np.sort(rng.choice(LIST_TASKS, 256, replace=False)))
+    O.build()
+    X2h = O.norms(L["X"])
+    okers = [O.make_kernel(t, **p) for t, p in sub["specs"]]
+    u_ref = np.zeros(LIST_POOL)
+    O.dgsks_list(okers[0], u_ref, sub["a_off"], sub["a_idx"], sub["a_idx"], sub["b_off"], sub["b_idx"],
+                 sub["b_idx"], L["X"], X2h, L["X"], X2h, L["w"], kers=okers)
+    cond = np.zeros(LIST_POOL)
+    for t in range(len(sub["specs"])):
+        a0, a1, b0, b1 = sub["a_off"][t], sub["a_off"][t + 1], sub["b_off"][t], sub["b_off"][t + 1]
+        amap, bmap = sub["a_idx"][a0:a1], sub["b_idx"][b0:b1]
+        _, c = O.rows(okers[t], np.arange(a1 - a0, dtype=np.int32), L["X"], X2h, amap, L["X"], X2h, bmap,
+                      L["w"], bmap)
+        np.add.at(cond, amap, c)
+    named = np.unique(sub["a_idx"])
+    err = {"tasks_checked": 256, "pairs_checked": sub["pairs"],
+           "metrics": "normwise; cond = max over u entries of |du| / sum |K w| of the positions naming it"}
+    skers = [gsks.make_kernel(t, **p) for t, p in sub["specs"]]
+    for form in forms:
+        gsks.set_precision(prec_of(gsks, form))
+        u = torch.zeros(LIST_POOL, dtype=torch.float64, device="cuda")
+        call(sub, u, skers)
+        torch.cuda.synchronize()
+        e = O.errors(u.cpu().numpy()[named], u_ref[named], cond=cond[named])
+        err[form] = {k: float("%.3g" % v) for k, v in e.items()}
+    gsks.set_precision(gsks.GSKS_FP64)
+    out["error"] = err
+
+    # CPU baseline: the oracle's OpenMP list driver on a bounded subset of tasks
+    if not args.no_cpu:
+        cores = os.cpu_count() or 1
+        O.set_threads(cores)
+        order = rng.permutation(LIST_TASKS)
+
+        def timed(ntk):
+            s2 = _sub_list(L, np.sort(order[:ntk]))
+            ok = [O.make_kernel(t, **p) for t, p in s2["specs"]]
+            u = np.zeros(LIST_POOL)
+            t0 = time.perf_counter()
+            O.dgsks_list(ok[0], u, s2["a_off"], s2["a_idx"], s2["a_idx"], s2["b_off"], s2["b_idx"], s2["b_idx"],
+                         L["X"], X2h, L["X"], X2h, L["w"], kers=ok, impl="omp")
+            return time.perf_counter() - t0, s2["pairs"]
+
+        timed(16)                                              # thread start-up
+        t1, p1 = timed(256)
+        ntk = int(min(LIST_TASKS, max(256, 256 * args.cpu_seconds / max(t1, 1e-3))))
+        t, pairs = timed(ntk)
+        out["cpu_baseline"] = {"value": pairs / t, "unit": "pair-evals/s", "cores": cores, "kind": "port",
+                               "sample": f"{ntk} random tasks of the list ({pairs:.3g} pairs, {t:.1f} s)",
+                               "impl": "oracle_dgsks_list_omp (restated frame/omp_dgsks_list.cpp driver over "
+                                       "oracle_dgsks_fused)"}
+    return out
 
 
 def run_e2e(args, torch, gsks, wl, ws, form):

@@ -357,3 +357,68 @@ int oracle_dgsks_list(ks_t *ker, ks_t *kers, int ntask, int k, double *u,
   }
   return 0;
 }
+
+/* Multi-threaded batched evaluation (the timed CPU baseline of the batched
+ * workload), after frame/omp_dgsks_list.cpp:297-420: the reference assigns
+ * tasks greedily, largest cost first, to the least loaded of its threads and
+ * runs one dgsks per task into a per-thread copy of u, then adds the copies.
+ * Here the threads take the tasks in descending cost order from a shared
+ * queue (the same balance without the ahead-of-time assignment), each task
+ * runs oracle_dgsks_fused single-threaded into the thread's copy of u, and the
+ * copies are added into u.  Arguments as oracle_dgsks_list; nu = size of u. */
+static const int *g_cost_a, *g_cost_b;
+static int cost_cmp(const void *x, const void *y)
+{
+  const int tx = *(const int *)x, ty = *(const int *)y;
+  const long long cx = (long long)(g_cost_a[tx + 1] - g_cost_a[tx]) * (g_cost_b[tx + 1] - g_cost_b[tx]);
+  const long long cy = (long long)(g_cost_a[ty + 1] - g_cost_a[ty]) * (g_cost_b[ty + 1] - g_cost_b[ty]);
+  return cx < cy ? 1 : (cx > cy ? -1 : (tx - ty));
+}
+
+int oracle_dgsks_list_omp(ks_t *ker, ks_t *kers, int ntask, int k, double *u, int nu,
+                          const int *a_off, const int *a_idx, const int *u_idx,
+                          const int *b_off, const int *b_idx, const int *w_idx,
+                          const double *XA, const double *XA2,
+                          const double *XB, const double *XB2, const double *w)
+{
+  int *order = (int *)malloc(sizeof(int) * (size_t)(ntask > 0 ? ntask : 1));
+  if (!order) return -2;
+  for (int t = 0; t < ntask; t++) order[t] = t;
+  g_cost_a = a_off; g_cost_b = b_off;
+  qsort(order, (size_t)ntask, sizeof(int), cost_cmp);
+  int nthr = 1;
+#ifdef _OPENMP
+  nthr = omp_get_max_threads();
+#endif
+  double *ucopy = (double *)calloc((size_t)nthr * (size_t)nu, sizeof(double));
+  if (!ucopy) { free(order); return -2; }
+  int rc = 0;
+  #pragma omp parallel
+  {
+    int me = 0;
+#ifdef _OPENMP
+    me = omp_get_thread_num();
+#endif
+    double *um = ucopy + (size_t)me * nu;
+    #pragma omp for schedule(dynamic, 1)
+    for (int q = 0; q < ntask; q++) {
+      const int t = order[q];
+      const int ma = a_off[t + 1] - a_off[t], nb = b_off[t + 1] - b_off[t];
+      if (ma == 0 || nb == 0) continue;
+      ks_t kt = kers ? kers[t] : *ker;
+      const int r = oracle_dgsks_fused(&kt, ma, nb, k, um, u_idx + a_off[t], XA, XA2, a_idx + a_off[t],
+                                       XB, XB2, b_idx + b_off[t], w, w_idx + b_off[t]);
+      if (r) {
+        #pragma omp atomic write
+        rc = r;
+      }
+    }
+  }
+  #pragma omp parallel for
+  for (int e = 0; e < nu; e++)
+    for (int q = 0; q < nthr; q++) u[e] += ucopy[(size_t)q * nu + e];
+  free(ucopy);
+  free(order);
+  return rc;
+}
+

@@ -149,7 +149,10 @@ def rows(ker: KsT, rows_idx, XA, XA2, amap, XB, XB2, bmap, w, wmap):
 
 def dgsks_list(ker: KsT, u, a_off, a_idx, u_idx, b_off, b_idx, w_idx, XA, XA2, XB, XB2, w,
                kers=None, impl="oracle") -> int:
-    """Batched evaluation over CSR task lists, accumulating into u."""
+    """Batched evaluation over CSR task lists, accumulating into u.
+
+    impl: "oracle" (serial restatement), "omp" (multi-threaded restatement of
+    the reference's OpenMP list driver, the CPU baseline) or "reference"."""
     k = int(XA.shape[1])
     ntask = int(a_off.size - 1)
     if impl == "oracle":
@@ -158,6 +161,14 @@ def dgsks_list(ker: KsT, u, a_off, a_idx, u_idx, b_off, b_idx, w_idx, XA, XA2, X
             karr = (KsT * ntask)(*kers)
         return int(_lib("oracle").oracle_dgsks_list(
             C.byref(ker), karr, C.c_int(ntask), C.c_int(k), _p(u),
+            _p(a_off), _p(a_idx), _p(u_idx), _p(b_off), _p(b_idx), _p(w_idx),
+            _p(XA), _p(XA2), _p(XB), _p(XB2), _p(w)))
+    if impl == "omp":
+        karr = None
+        if kers is not None:
+            karr = (KsT * ntask)(*kers)
+        return int(_lib("oracle").oracle_dgsks_list_omp(
+            C.byref(ker), karr, C.c_int(ntask), C.c_int(k), _p(u), C.c_int(u.size),
             _p(a_off), _p(a_idx), _p(u_idx), _p(b_off), _p(b_idx), _p(w_idx),
             _p(XA), _p(XA2), _p(XB), _p(XB2), _p(w)))
     if impl == "reference":

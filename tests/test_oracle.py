@@ -68,6 +68,12 @@ def test_list_oracle_matches_reference(oracle_mod, name):
     # the reference's own per-entry check is 1e-10 (test/test_dgsks_list.cpp:241-247)
     assert O.errors(g["u_list"], g["u_ref"])["normwise"] <= 1e-12
     assert O.errors(u, g["u_list"])["normwise"] <= 1e-12
+    # the multi-threaded list baseline (per-thread copies of u, then a merge)
+    u2 = g["u0"].copy()
+    assert O.dgsks_list(O.make_kernel(meta["type"], **meta["params"]), u2, g["a_off"], g["a_idx"], g["a_idx"],
+                        g["b_off"], g["b_idx"], g["b_idx"], g["X"], g["X2"], g["X"], g["X2"], g["w"],
+                        impl="omp") == 0
+    assert O.errors(u2, g["u_list"])["normwise"] <= 1e-12
 
 
 def test_illegal_type_reports(oracle_mod):
