@@ -76,8 +76,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--case", default=None, choices=[k[0] for k in KERNELS],
-                    help="profiling case: only device calls of one kernel type (for ncu)")
+    ap.add_argument("--case", default=None, choices=[k[0] for k in KERNELS] + ["list"],
+                    help="profiling case: only device calls of one kernel type, or the batched "
+                         "workload with --tasks tasks (for ncu)")
+    ap.add_argument("--tasks", type=int, default=2000, help="tasks of --case list")
     ap.add_argument("--precision", default="split", choices=["fp64", "split"], help="form of --case")
     ap.add_argument("--m", type=int, default=M_T)
     ap.add_argument("--n", type=int, default=N_S)
@@ -207,6 +209,21 @@ def run_case(args):
         B.build()
     from ks_gb300 import gsks
     torch.cuda.set_device(0)
+    if args.case == "list":
+        import numpy as np
+        L = make_list_workload(ntask=args.tasks)
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        X, w = dev(L["X"]), dev(L["w"])
+        kers = [gsks.make_kernel(t, **p) for t, p in L["specs"]]
+        gsks.set_precision(prec_of(gsks, args.precision))
+        u = torch.zeros(LIST_POOL, dtype=torch.float64, device="cuda")
+        for _ in range(args.reps):
+            gsks.dgsks_list(kers[0], u, dev(L["a_off"]), dev(L["a_idx"]), dev(L["b_off"]), dev(L["b_idx"]),
+                            X, None, X, None, w, kers=kers)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": "list", "tasks": args.tasks, "pairs": L["pairs"], "reps": args.reps,
+                          "precision": args.precision, "u_norm": float(u.norm())}))
+        return
     wl = make_workload(torch)
     name, kt, p, _f = [k for k in KERNELS if k[0] == args.case][0]
     u = torch.zeros(M_T, dtype=torch.float64, device="cuda")
