@@ -5,7 +5,7 @@
 // is kept for the squared norms, for the distance of pairs flagged by an
 // error bound, and for the per-target accumulation of u.
 //
-// Operand split (per call, in FP64, in split_pack):
+// Operand split (per call, pack_kernel):
 //   x'' = alpha (x - c)            c: centre of the call's bounding box (distance
 //                                  kernels; 0 for polynomial / tanh); alpha folds
 //                                  the Gaussian scale: alpha^2 = -scal log2(e)
@@ -18,25 +18,31 @@
 // The next terms (a1 b2 + a2 b1 + a2 b2 + a1 b3 + a3 b1, 2^-8 and below
 // relative) go to a second accumulator "L".  x''.y'' = sigma^2 2^-14 (H + L).
 //
-// Epilogue (one thread per target row, 128 rows = the 128 TMEM lanes):
+// Epilogue (one thread per target row and 32-column group):
 //   d2 = |x''|^2 + |y''|^2 - 2 x''.y'' assembled as an unevaluated FP32 sum
 //   t + lo: the norms are split on a common grid so that their high parts add
 //   exactly, -2 sigma^2 2^-14 H is exact, and Fast2Sum captures the last
-//   rounding (|x''|^2 + |y''|^2 >= |2 x''.y''|).  The Gaussian value is
-//   2^-t (1 - ln2 lo) with the SFU's ex2.  Pairs whose distance the bound says
-//   is not resolved (Laplace near coincidence; cancellation when the points sit
-//   far from the centre) are recomputed in FP64 from the pool coordinates.
-// Row sums: FP32 within a 128-source tile (4 interleaved partial sums), FP64
-// across tiles; one partial per (row, source chunk); a fixed-order reduction
-// adds the partials into u (deterministic).
+//   rounding.  Gaussian-type values are 2^-t (1 - ln2 lo) with the SFU's ex2,
+//   Laplace values come from a table-driven log2 with an exact integer
+//   exponent.  Pairs whose distance an error bound says is not resolved
+//   (Laplace near coincidence; narrow bandwidths relative to the data's extent)
+//   are recomputed from the pool coordinates, and rows whose values over a
+//   32-column group all fall below the FP32 range are redone in FP64.
+// Row sums: FP32 within a 32-column group (4 interleaved partial sums), FP64
+// across groups and tiles; one partial per (row, source chunk); a fixed-order
+// reduction adds the partials into u (deterministic).
 //
-// Pipeline (one CTA per SM, persistent over (target tile, source chunk) items):
-//   warp 0      producer: bulk copies (TMA engine) of the target tile image
-//               (resident for the item) and of the source tile images (2 stages)
-//   warp 1      MMA issuer: 6 x k/16 tcgen05.mma per source tile into one of
-//               two TMEM accumulator pairs (double buffered)
-//   warps 2..5  epilogue: tcgen05.ld of the accumulators, kernel function,
-//               weighted row sums
+// Pipeline (one CTA per SM, persistent over work items = (target tile, run of
+// source tiles)):
+//   warp 0       producer: bulk copies (TMA engine) of the target tile image,
+//                resident for the item when k <= 64 (3 source stages), else
+//                both operands streamed in 64-wide k chunks (2 stages)
+//   warp 1       MMA issuer: 6 tcgen05.mma per 16-wide k step into one of two
+//                TMEM accumulator pairs (double buffered, 512 columns)
+//   warps 2..17  epilogue: 4 column groups x 4 TMEM sub-partitions, tcgen05.ld
+//                of 16 columns at a time, kernel function, weighted row sums
+// The batched form (KS_LIST) runs the same pipeline over a table of items
+// from many tasks, each task with its own tiles, kernel and thresholds.
 // Every wait is bounded; on a timeout the CTA records an error, drains and
 // frees its tensor memory.
 #include "gsks.h"
