@@ -74,14 +74,29 @@ constexpr int NTHREADS = 32 * (2 + EPI_WARPS);
 constexpr long long WAIT_LIMIT = 1LL << 32;   // clock cycles (~2 s) per wait
 constexpr uint32_t TMEM_COLS = 512;           // 2 buffers x (H, L) x 128 columns
 
-struct PtMeta {          // 32 bytes per point, appended to each tile image
+struct PtMeta {          // target tiles: 32 bytes per point, appended to the image
   float n_hi, n_lo;      // |x''|^2 = n_hi + n_lo, n_hi on the call's grid q
-  float w;               // sources: w[wmap[j]]; targets: unused
-  float h;               // var-bandwidth factor (targets: -0.5 log2e hi; sources: hj)
-  int pos;               // position in amap / bmap, -1 for padding
-  int pad[3];            // [0] sources, column 32g: bits of sum |w| over columns 32g..32g+31
-                         // [1] var-bandwidth: low part of h (float bits)
+  float w;               // unused
+  float h;               // var-bandwidth factor -0.5 log2e hi (gfast: the row factor)
+  int pos;               // position in amap, -1 for padding
+  int pad[3];            // [1] var-bandwidth: low part of h (float bits)
 };
+
+// Source tiles: the same 32 bytes per point as a structure of arrays, so that
+// one 16-byte shared-memory load serves four columns of one field.
+struct SrcMeta {
+  float n_hi[BN], n_lo[BN];
+  float w[BN];           // w[wmap[j]] (gfast: times the column's low-norm factor)
+  float h[BN];           // var-bandwidth factor hj
+  int pos[BN];           // position in bmap, -1 for padding
+  float wsum[BN];        // column 32g: sum of |w| over columns 32g..32g+31
+  float hlo[BN];         // var-bandwidth: low part of h
+  int pad[BN];
+};
+static_assert(sizeof(SrcMeta) == BN * sizeof(PtMeta), "both metadata blocks take 32 bytes per point");
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *(const float4 *)p; }
+__device__ __forceinline__ float f4(const float4 &v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
 
 // Laplace: K = scal d2^powe = 2^(log2 scal + powe log2 d2), powe = -P/2,
 // log2 scal = ls13 2^-13 + lsf.
@@ -481,13 +496,21 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
     mt.h = (float)hv;
     mt.pad[1] = __float_as_int((float)(hv - (double)mt.h));
   }
+  if (side == 0) {
+    ((PtMeta *)(base + NBLK * bb))[r] = mt;
+    return;
+  }
   // sources: sum of |w| over each group of 32 columns, kept with the group's
   // first column (the underflow test of the exponential kernels)
   float wa = fabsf(mt.w);
 #pragma unroll
   for (int o = 16; o; o >>= 1) wa += __shfl_xor_sync(0xffffffffu, wa, o);
-  if ((r & 31) == 0) mt.pad[0] = __float_as_int(wa);
-  ((PtMeta *)(base + NBLK * bb))[r] = mt;
+  SrcMeta *sm = (SrcMeta *)(base + NBLK * bb);
+  sm->n_hi[r] = mt.n_hi; sm->n_lo[r] = mt.n_lo; sm->w[r] = mt.w; sm->h[r] = mt.h;
+  sm->pos[r] = mt.pos;
+  sm->wsum[r] = (r & 31) == 0 ? wa : 0.0f;
+  sm->hlo[r] = __int_as_float(mt.pad[1]);
+  sm->pad[r] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -796,28 +819,31 @@ __device__ __forceinline__ void assemble(float H, float L, float an_hi, float an
 // source weights and the row factor: kv = 2^-(g tt) (1 - ln2 g ee).
 template <int NC>
 __device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
-                                                const PtMeta *__restrict__ bm, float an_hi, float rc,
+                                                const SrcMeta *__restrict__ bm, int c0, float an_hi, float rc,
                                                 float (&acc)[4])
 {
   const float cg = 0.69314718f * rc;          // -ln2 g
 #pragma unroll
-  for (int j = 0; j < NC; j++) {
-    const float4 m0 = *(const float4 *)&bm[j];   // nu_hi, 0, w', h
-    const float w = m0.z;
-    const float H = __uint_as_float(h[j]), L = __uint_as_float(l[j]);
-    const float t1 = (an_hi + m0.x) - H;      // exact
-    const float tt = t1 - L;
-    const float ee = (t1 - tt) - L;
-    const float e = ex2_approx(tt * rc);      // 2^-(g tt)
-    const float kv = fmaf(e, cg * ee, e);
-    acc[j & 3] = fmaf(kv, w, acc[j & 3]);
+  for (int j4 = 0; j4 < NC; j4 += 4) {
+    const float4 nh = ld4(&bm->n_hi[c0 + j4]), ww = ld4(&bm->w[c0 + j4]);   // nu_hi, w'
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int j = j4 + q;
+      const float H = __uint_as_float(h[j]), L = __uint_as_float(l[j]);
+      const float t1 = (an_hi + f4(nh, q)) - H;   // exact
+      const float tt = t1 - L;
+      const float ee = (t1 - tt) - L;
+      const float e = ex2_approx(tt * rc);        // 2^-(g tt)
+      const float kv = fmaf(e, cg * ee, e);
+      acc[q] = fmaf(kv, f4(ww, q), acc[q]);
+    }
   }
 }
 
 // NC columns of one row, distance kernels.  Returns the flagged columns.
 template <int KT, bool EXACT, bool FLAGS, int NC>
 __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
-                                              const PtMeta *__restrict__ bm, const PtMeta &am, float rc,
+                                              const SrcMeta *__restrict__ bm, int c0, const PtMeta &am, float rc,
                                               const TaskParam &T, const float4 *__restrict__ ltab,
                                               float (&acc)[4])
 {
@@ -826,30 +852,38 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
   float t_flag = 0.f, rho = 0.f;
   if constexpr (FLAGS) { t_flag = T.t_flag; rho = T.rho; }
 #pragma unroll
-  for (int j = 0; j < NC; j++) {
-    const float4 m0 = *(const float4 *)&bm[j];   // n_hi, n_lo, w, h
-    float t, lo, s;
-    assemble<EXACT>(__uint_as_float(h[j]), __uint_as_float(l[j]), am.n_hi, am.n_lo, m0.x, m0.y, rc, t, lo, s);
-    float kv;
-    if constexpr (KT == KS_LAPLACE) kv = laplace_val(t, lo, ltab, T.lap);
-    else if constexpr (KT == KS_GAUSS_UNSCALED) kv = exp2_prod(t, lo, T.s2, T.s2l);
-    else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
-      // factor h_i h_j (negative) as a float pair
-      const float ph = am.h * m0.w;
-      const float pl = fmaf(am.h, m0.w, -ph) +
-                       fmaf(am.h, __int_as_float(bm[j].pad[1]), __int_as_float(am.pad[1]) * m0.w);
-      kv = exp2_prod(t, lo, ph, pl);
-    } else kv = kval32<KT>(t, lo, 0.f, am.h, m0.w, kp);
-    if constexpr (FLAGS) {
-      if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
-        const float f = -am.h * m0.w;             // 0.5 log2(e) h_i h_j
-        if (f > t_flag && t * f < 126.f) { flags |= 1u << j; kv = 0.f; }
-      } else {
-        if (t < t_flag || t < rho * s) { flags |= 1u << j; kv = 0.f; }
+  for (int j4 = 0; j4 < NC; j4 += 4) {
+    const float4 nh = ld4(&bm->n_hi[c0 + j4]), nl = ld4(&bm->n_lo[c0 + j4]);
+    const float4 ww = ld4(&bm->w[c0 + j4]);
+    float4 hh = make_float4(0.f, 0.f, 0.f, 0.f), hl = hh;
+    if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) { hh = ld4(&bm->h[c0 + j4]); hl = ld4(&bm->hlo[c0 + j4]); }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int j = j4 + q;
+      float t, lo, s;
+      assemble<EXACT>(__uint_as_float(h[j]), __uint_as_float(l[j]), am.n_hi, am.n_lo, f4(nh, q), f4(nl, q), rc, t,
+                      lo, s);
+      float kv;
+      if constexpr (KT == KS_LAPLACE) kv = laplace_val(t, lo, ltab, T.lap);
+      else if constexpr (KT == KS_GAUSS_UNSCALED) kv = exp2_prod(t, lo, T.s2, T.s2l);
+      else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
+        // factor h_i h_j (negative) as a float pair
+        const float hc = f4(hh, q);
+        const float ph = am.h * hc;
+        const float pl = fmaf(am.h, hc, -ph) + fmaf(am.h, f4(hl, q), __int_as_float(am.pad[1]) * hc);
+        kv = exp2_prod(t, lo, ph, pl);
+      } else kv = kval32<KT>(t, lo, 0.f, am.h, 0.f, kp);
+      if constexpr (FLAGS) {
+        if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
+          const float f = -am.h * f4(hh, q);      // 0.5 log2(e) h_i h_j
+          if (f > t_flag && t * f < 126.f) { flags |= 1u << j; kv = 0.f; }
+        } else {
+          if (t < t_flag || t < rho * s) { flags |= 1u << j; kv = 0.f; }
+        }
       }
+      // padding columns carry w = 0 and finite distances
+      acc[q] = fmaf(kv, f4(ww, q), acc[q]);
     }
-    // padding columns carry w = 0 and finite distances
-    acc[j & 3] = fmaf(kv, m0.z, acc[j & 3]);
   }
   return flags;
 }
@@ -857,22 +891,26 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
 // NC columns of one row, inner-product kernels (polynomial, tanh).
 template <int KT, int NC>
 __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
-                                             const PtMeta *__restrict__ bm, int valid, float rc,
+                                             const SrcMeta *__restrict__ bm, int c0, int valid, float rc,
                                              const KParams &kp, float (&acc)[4])
 {
 #pragma unroll
-  for (int j = 0; j < NC; j++) {
-    const float w = bm[j].w;
-    const float cc = fmaf(__uint_as_float(l[j]), rc, __uint_as_float(h[j]) * rc) * -0.5f;  // x.y
-    const float kv = kval32<KT>(0.f, 0.f, cc, 0.f, 0.f, kp);
-    acc[j & 3] += (j < valid) ? kv * w : 0.f;      // the kernel of a padding column may be NaN
+  for (int j4 = 0; j4 < NC; j4 += 4) {
+    const float4 ww = ld4(&bm->w[c0 + j4]);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int j = j4 + q;
+      const float cc = fmaf(__uint_as_float(l[j]), rc, __uint_as_float(h[j]) * rc) * -0.5f;  // x.y
+      const float kv = kval32<KT>(0.f, 0.f, cc, 0.f, 0.f, kp);
+      acc[q] += (j < valid) ? kv * f4(ww, q) : 0.f;   // the kernel of a padding column may be NaN
+    }
   }
 }
 
 // Test hook: raw accumulators and epilogue values of NC columns from c0.
 template <int KT, int NC>
 __device__ void dump_chunk(float *dump, int row, int c0, const uint32_t (&h)[NC], const uint32_t (&l)[NC],
-                           const PtMeta *bm, const PtMeta &am, float rc, const KParams &kp)
+                           const SrcMeta *bm, const PtMeta &am, float rc, const KParams &kp)
 {
   for (int j = 0; j < NC; j++) {
     const int c = c0 + j;
@@ -881,9 +919,9 @@ __device__ void dump_chunk(float *dump, int row, int c0, const uint32_t (&h)[NC]
     dp[0] = H; dp[1] = L;
     if constexpr (kt_uses_norms(KT)) {
       float t, lo, s;
-      assemble<false>(H, L, am.n_hi, am.n_lo, bm[j].n_hi, bm[j].n_lo, rc, t, lo, s);
+      assemble<false>(H, L, am.n_hi, am.n_lo, bm->n_hi[c], bm->n_lo[c], rc, t, lo, s);
       dp[2] = 0.f;
-      if constexpr (KT != KS_LAPLACE) dp[2] = kval32<KT>(t, lo, 0.f, am.h, bm[j].h, kp);
+      if constexpr (KT != KS_LAPLACE) dp[2] = kval32<KT>(t, lo, 0.f, am.h, bm->h[c], kp);
       dp[3] = t; dp[4] = lo;
     } else {
       dp[2] = kval32<KT>(0.f, 0.f, fmaf(L, rc, H * rc) * -0.5f, 0.f, 0.f, kp);
@@ -906,7 +944,7 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 // one add: FP64 instructions issue at a small fraction of the FP32 rate here.
 template <int KT>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
-                                              const PtMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
+                                              const SrcMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
                                               bool gfast, bool dump, const float4 *ltab, double &racc)
 {
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
@@ -920,19 +958,19 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     tmem_ld16(tH + c0, h);
     tmem_ld16(tH + 128 + c0, l);
     tmem_ld_wait();
-    if (dump) dump_chunk<KT, 16>(a.dump, row, c0, h, l, bm + c0, am, rc, T.kp);
+    if (dump) dump_chunk<KT, 16>(a.dump, row, c0, h, l, bm, am, rc, T.kp);
     if constexpr (KT == KS_GAUSSIAN) {
-      if (gfast) { epi_chunk_gfast<16>(h, l, bm + c0, am.n_hi, rc, acc); continue; }
+      if (gfast) { epi_chunk_gfast<16>(h, l, bm, c0, am.n_hi, rc, acc); continue; }
     }
     if constexpr (kt_uses_norms(KT)) {
       uint32_t flags = 0;
       const bool fl = T.any_flag != 0;
       if (exact) {
-        if (fl) flags = epi_chunk<KT, true, true, 16>(h, l, bm + c0, am, rc, T, ltab, acc);
-        else epi_chunk<KT, true, false, 16>(h, l, bm + c0, am, rc, T, ltab, acc);
+        if (fl) flags = epi_chunk<KT, true, true, 16>(h, l, bm, c0, am, rc, T, ltab, acc);
+        else epi_chunk<KT, true, false, 16>(h, l, bm, c0, am, rc, T, ltab, acc);
       } else {
-        if (fl) flags = epi_chunk<KT, false, true, 16>(h, l, bm + c0, am, rc, T, ltab, acc);
-        else epi_chunk<KT, false, false, 16>(h, l, bm + c0, am, rc, T, ltab, acc);
+        if (fl) flags = epi_chunk<KT, false, true, 16>(h, l, bm, c0, am, rc, T, ltab, acc);
+        else epi_chunk<KT, false, false, 16>(h, l, bm, c0, am, rc, T, ltab, acc);
       }
       // FP64 rechecks of the flagged pairs of these 16 columns
       while (flags) {
@@ -940,14 +978,14 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
         flags &= flags - 1;
         const int c = c0 + j;
         if (c < ncols && am.pos >= 0) {
-          const double v = recheck<KT>(a, T, ltab, am.pos, bm[c].pos);
+          const double v = recheck<KT>(a, T, ltab, am.pos, bm->pos[c]);
           rchk += v;
           fchk += fabsf((float)v);
           nchk = true;
         }
       }
     } else {
-      epi_chunk_ip<KT, 16>(h, l, bm + c0, ncols - c0, rc, T.kp, acc);
+      epi_chunk_ip<KT, 16>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
     }
   }
   const float fs = (acc[0] + acc[1]) + (acc[2] + acc[3]);
@@ -955,11 +993,11 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     // A row whose kernel values over these 32 columns all lie below 2^-96
     // (FP32 flushes values below 2^-126 to zero, FP64 keeps them down to
     // 2^-1074) takes these pairs from FP64 instead, flagged pairs included.
-    const float W = __int_as_float(bm[grp * 32].pad[0]);
+    const float W = bm->wsum[grp * 32];
     if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W) {
       double r = 0.0;
       const int c1 = min(grp * 32 + 32, ncols);
-      for (int c = grp * 32; c < c1; c++) r += recheck<KT>(a, T, ltab, am.pos, bm[c].pos);
+      for (int c = grp * 32; c < c1; c++) r += recheck<KT>(a, T, ltab, am.pos, bm->pos[c]);
       if constexpr (KT == KS_GAUSSIAN) {
         if (gfast) r /= (double)am.h;   // the caller applies the row factor to the row sum
       }
@@ -1148,7 +1186,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         if (!mbar_wait(&S->t_full[buf], (tc >> 1) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
         if (!mbar_wait(&S->m_full[ms], (g / NMETA) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
         tc_fence_after();
-        const PtMeta *bm = (const PtMeta *)(sBm + ms * meta_bytes);
+        const SrcMeta *bm = (const SrcMeta *)(sBm + ms * meta_bytes);
         const int ncols = a.tab ? a.btile_cols[tj] : min(BN, a.n - tj * BN);
         const uint32_t tH = tmem + ((uint32_t)(qd * 32) << 16) + buf * 256;
         const bool dump = a.dump && blockIdx.x == 0 && tc == 0;
