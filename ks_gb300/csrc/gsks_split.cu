@@ -815,6 +815,30 @@ __device__ __forceinline__ void assemble(float H, float L, float an_hi, float an
   s *= -rc;
 }
 
+// assemble for two columns at once (packed FP32 pairs; the same operations and
+// roundings per column).  NRC = (-rc, -rc).
+template <bool EXACT>
+__device__ __forceinline__ void assemble2(uint64_t H, uint64_t L, uint64_t AN, uint64_t ANL, uint64_t BN,
+                                          uint64_t BNL, uint64_t NRC, uint64_t &T, uint64_t &LO, uint64_t &S)
+{
+  const uint64_t s = add2(AN, BN);
+  uint64_t tt, ee;
+  if constexpr (EXACT) {
+    const uint64_t t1 = sub2(s, H);
+    tt = sub2(t1, L);
+    ee = sub2(sub2(t1, tt), L);
+  } else {
+    const uint64_t u1 = sub2(s, L);
+    const uint64_t e1 = sub2(sub2(s, u1), L);
+    tt = sub2(u1, H);
+    const uint64_t e2 = sub2(sub2(u1, tt), H);
+    ee = add2(e1, e2);
+  }
+  T = mul2(tt, NRC);
+  LO = mul2(add2(add2(ANL, BNL), ee), NRC);
+  S = mul2(s, NRC);
+}
+
 // NC columns of one row, Gaussian with the low norm parts folded into the
 // source weights and the row factor: kv = 2^-(g tt) (1 - ln2 g ee).
 template <int NC>
@@ -822,22 +846,30 @@ __device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const u
                                                 const SrcMeta *__restrict__ bm, int c0, float an_hi, float rc,
                                                 float (&acc)[4])
 {
+  // two columns per instruction (packed FP32 pairs); column j feeds acc[j & 3]
   const float cg = 0.69314718f * rc;          // -ln2 g
+  const uint64_t AN = pk2(an_hi, an_hi), RC = pk2(rc, rc), CG = pk2(cg, cg);
+  uint64_t A01 = pk2(acc[0], acc[1]), A23 = pk2(acc[2], acc[3]);
 #pragma unroll
   for (int j4 = 0; j4 < NC; j4 += 4) {
     const float4 nh = ld4(&bm->n_hi[c0 + j4]), ww = ld4(&bm->w[c0 + j4]);   // nu_hi, w'
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < 4; q += 2) {
       const int j = j4 + q;
-      const float H = __uint_as_float(h[j]), L = __uint_as_float(l[j]);
-      const float t1 = (an_hi + f4(nh, q)) - H;   // exact
-      const float tt = t1 - L;
-      const float ee = (t1 - tt) - L;
-      const float e = ex2_approx(tt * rc);        // 2^-(g tt)
-      const float kv = fmaf(e, cg * ee, e);
-      acc[q] = fmaf(kv, f4(ww, q), acc[q]);
+      const uint64_t H = pk2(__uint_as_float(h[j]), __uint_as_float(h[j + 1]));
+      const uint64_t L = pk2(__uint_as_float(l[j]), __uint_as_float(l[j + 1]));
+      const uint64_t t1 = sub2(add2(AN, pk2(f4(nh, q), f4(nh, q + 1))), H);   // exact
+      const uint64_t tt = sub2(t1, L);
+      const uint64_t ee = sub2(sub2(t1, tt), L);
+      const uint64_t ar = mul2(tt, RC);
+      const uint64_t E = pk2(ex2_approx(lo2(ar)), ex2_approx(hi2(ar)));       // 2^-(g tt)
+      const uint64_t kv = fma2(E, mul2(CG, ee), E);
+      const uint64_t W = pk2(f4(ww, q), f4(ww, q + 1));
+      if (q == 0) A01 = fma2(kv, W, A01);
+      else A23 = fma2(kv, W, A23);
     }
   }
+  acc[0] = lo2(A01); acc[1] = hi2(A01); acc[2] = lo2(A23); acc[3] = hi2(A23);
 }
 
 // NC columns of one row, distance kernels.  Returns the flagged columns.
@@ -851,18 +883,28 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
   uint32_t flags = 0;
   float t_flag = 0.f, rho = 0.f;
   if constexpr (FLAGS) { t_flag = T.t_flag; rho = T.rho; }
+  const uint64_t AN = pk2(am.n_hi, am.n_hi), ANL = pk2(am.n_lo, am.n_lo), NRC = pk2(-rc, -rc);
 #pragma unroll
   for (int j4 = 0; j4 < NC; j4 += 4) {
     const float4 nh = ld4(&bm->n_hi[c0 + j4]), nl = ld4(&bm->n_lo[c0 + j4]);
     const float4 ww = ld4(&bm->w[c0 + j4]);
     float4 hh = make_float4(0.f, 0.f, 0.f, 0.f), hl = hh;
     if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) { hh = ld4(&bm->h[c0 + j4]); hl = ld4(&bm->hlo[c0 + j4]); }
+    uint64_t T2[2], LO2[2], S2[2];
+#pragma unroll
+    for (int p2 = 0; p2 < 2; p2++) {
+      const int j = j4 + 2 * p2;
+      assemble2<EXACT>(pk2(__uint_as_float(h[j]), __uint_as_float(h[j + 1])),
+                       pk2(__uint_as_float(l[j]), __uint_as_float(l[j + 1])), AN, ANL,
+                       pk2(f4(nh, 2 * p2), f4(nh, 2 * p2 + 1)), pk2(f4(nl, 2 * p2), f4(nl, 2 * p2 + 1)), NRC,
+                       T2[p2], LO2[p2], S2[p2]);
+    }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       const int j = j4 + q;
-      float t, lo, s;
-      assemble<EXACT>(__uint_as_float(h[j]), __uint_as_float(l[j]), am.n_hi, am.n_lo, f4(nh, q), f4(nl, q), rc, t,
-                      lo, s);
+      const float t = (q & 1) ? hi2(T2[q >> 1]) : lo2(T2[q >> 1]);
+      const float lo = (q & 1) ? hi2(LO2[q >> 1]) : lo2(LO2[q >> 1]);
+      const float s = (q & 1) ? hi2(S2[q >> 1]) : lo2(S2[q >> 1]);
       float kv;
       if constexpr (KT == KS_LAPLACE) kv = laplace_val(t, lo, ltab, T.lap);
       else if constexpr (KT == KS_GAUSS_UNSCALED) kv = exp2_prod(t, lo, T.s2, T.s2l);
@@ -894,17 +936,46 @@ __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint
                                              const SrcMeta *__restrict__ bm, int c0, int valid, float rc,
                                              const KParams &kp, float (&acc)[4])
 {
+  // two columns per instruction where the kernel allows it (packed FP32 pairs)
+  const uint64_t RC = pk2(rc, rc), MH = pk2(-0.5f, -0.5f);
+  const float sc = (float)kp.scal, cn = (float)kp.cons;
+  const uint64_t SC = pk2(sc, sc), CN = pk2(cn, cn);
+  const bool ipow = KT == KS_POLYNOMIAL && kp.pmode == POW_INT;
+  uint64_t A[2] = {pk2(acc[0], acc[1]), pk2(acc[2], acc[3])};
 #pragma unroll
   for (int j4 = 0; j4 < NC; j4 += 4) {
     const float4 ww = ld4(&bm->w[c0 + j4]);
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const int j = j4 + q;
-      const float cc = fmaf(__uint_as_float(l[j]), rc, __uint_as_float(h[j]) * rc) * -0.5f;  // x.y
-      const float kv = kval32<KT>(0.f, 0.f, cc, 0.f, 0.f, kp);
-      acc[q] += (j < valid) ? kv * f4(ww, q) : 0.f;   // the kernel of a padding column may be NaN
+    for (int p2 = 0; p2 < 2; p2++) {
+      const int j = j4 + 2 * p2;
+      const uint64_t H = pk2(__uint_as_float(h[j]), __uint_as_float(h[j + 1]));
+      const uint64_t L = pk2(__uint_as_float(l[j]), __uint_as_float(l[j + 1]));
+      const uint64_t CC = mul2(fma2(L, RC, mul2(H, RC)), MH);          // x.y
+      float k0, k1;
+      if (ipow) {
+        // (scal x.y + cons)^p by binary powering on both columns
+        const uint64_t V = fma2(SC, CC, CN);
+        int e = kp.pint < 0 ? -kp.pint : kp.pint;
+        uint64_t R = pk2(1.0f, 1.0f), B = V;
+        for (;;) {
+          if (e & 1) R = mul2(R, B);
+          e >>= 1;
+          if (!e) break;
+          B = mul2(B, B);
+        }
+        k0 = lo2(R); k1 = hi2(R);
+        if (kp.pint < 0) { k0 = 1.0f / k0; k1 = 1.0f / k1; }
+      } else {
+        k0 = kval32<KT>(0.f, 0.f, lo2(CC), 0.f, 0.f, kp);
+        k1 = kval32<KT>(0.f, 0.f, hi2(CC), 0.f, 0.f, kp);
+      }
+      // the kernel of a padding column may be NaN (its weight is 0)
+      if (j >= valid) k0 = 0.f;
+      if (j + 1 >= valid) k1 = 0.f;
+      A[p2] = fma2(pk2(k0, k1), pk2(f4(ww, 2 * p2), f4(ww, 2 * p2 + 1)), A[p2]);
     }
   }
+  acc[0] = lo2(A[0]); acc[1] = hi2(A[0]); acc[2] = lo2(A[1]); acc[3] = hi2(A[1]);
 }
 
 // Test hook: raw accumulators and epilogue values of NC columns from c0.
