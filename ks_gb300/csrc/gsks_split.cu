@@ -582,6 +582,7 @@ __device__ __forceinline__ const TaskParam &pick_task(const TaskParam &slot, con
   else return single;
 }
 
+
 // Laplace table: for i in [0, 256), c_i ~ 1 / (1 + (i + 1/2) / 256) with 12
 // significant bits (so that r = f c_i - 1 is exact up to one rounding of a
 // value below 2^-8.8), and -log2(c_i) as an integer on the 2^-12 grid (bits in
@@ -627,6 +628,31 @@ __device__ __forceinline__ float laplace_val(float t, float lo, const float4 *__
   return n >= -126 ? y * __int_as_float((n + 127) << 23) : 0.0f;
 }
 
+// laplace_val of two columns, the floating-point part in packed FP32 pairs.
+__device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const float4 *__restrict__ tab,
+                                                 const LapParam &L)
+{
+  const float t0 = lo2(T), t1 = hi2(T);
+  const uint32_t u0 = __float_as_uint(t0), u1 = __float_as_uint(t1);
+  const float4 b0 = tab[(u0 >> 15) & (LTAB - 1)], b1 = tab[(u1 >> 15) & (LTAB - 1)];
+  const uint64_t F = pk2(__uint_as_float((u0 & 0x007fffffu) | 0x3f800000u),
+                         __uint_as_float((u1 & 0x007fffffu) | 0x3f800000u));
+  const uint64_t R = fma2(F, pk2(b0.x, b1.x), pk2(-1.0f, -1.0f));
+  uint64_t Q = fma2(R, pk2(-0.36067376f, -0.36067376f), pk2(0.48089835f, 0.48089835f));
+  Q = fma2(R, Q, pk2(-0.72134752f, -0.72134752f));
+  Q = mul2(R, fma2(R, Q, pk2(1.44269504f, 1.44269504f)));
+  const uint64_t RT = pk2(rcp_approx(t0), rcp_approx(t1));
+  const uint64_t LLO = add2(add2(pk2(b0.y, b1.y), Q), mul2(mul2(LO, RT), pk2(1.44269504f, 1.44269504f)));
+  const int E0 = L.ls13 - L.P * (((int)(u0 >> 23) - 127) * 4096 + __float_as_int(b0.z));
+  const int E1 = L.ls13 - L.P * (((int)(u1 >> 23) - 127) * 4096 + __float_as_int(b1.z));
+  const uint64_t ARG = fma2(pk2((float)(E0 & 8191), (float)(E1 & 8191)), pk2(0x1p-13f, 0x1p-13f),
+                            fma2(pk2(L.mh, L.mh), LLO, pk2(L.lsf, L.lsf)));
+  const int n0 = E0 >> 13, n1 = E1 >> 13;
+  const float s0 = n0 >= -126 ? __int_as_float((n0 + 127) << 23) : 0.0f;
+  const float s1 = n1 >= -126 ? __int_as_float((n1 + 127) << 23) : 0.0f;
+  return mul2(pk2(ex2_approx(lo2(ARG)), ex2_approx(hi2(ARG))), pk2(s0, s1));
+}
+
 // 2^n y in FP64, n in the FP64 exponent range (beyond it, 0 or inf).
 __device__ __forceinline__ double scale2(float y, int n)
 {
@@ -644,6 +670,15 @@ __device__ __forceinline__ float exp2_prod(float t, float lo, float ph, float pl
   const float ae = fmaf(t, ph, -a) + fmaf(lo, ph, t * pl);
   const float e = ex2_approx(a);
   return fmaf(e, 0.69314718f * ae, e);
+}
+
+// exp2_prod of two columns in packed FP32 pairs.
+__device__ __forceinline__ uint64_t exp2_prod2(uint64_t T, uint64_t LO, uint64_t PH, uint64_t PL)
+{
+  const uint64_t A = mul2(T, PH);
+  const uint64_t AE = add2(fma2(T, PH, sub2(0, A)), fma2(LO, PH, mul2(T, PL)));
+  const uint64_t E = pk2(ex2_approx(lo2(A)), ex2_approx(hi2(A)));
+  return fma2(E, mul2(pk2(0.69314718f, 0.69314718f), AE), E);
 }
 
 // 2^((t + lo)(ph + pl)) as exp2_prod, returned in FP64 so that values below
@@ -899,6 +934,25 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
                        pk2(f4(nh, 2 * p2), f4(nh, 2 * p2 + 1)), pk2(f4(nl, 2 * p2), f4(nl, 2 * p2 + 1)), NRC,
                        T2[p2], LO2[p2], S2[p2]);
     }
+    uint64_t KV2[2] = {0, 0};
+    if constexpr (KT == KS_LAPLACE) {
+      KV2[0] = laplace_val2(T2[0], LO2[0], ltab, T.lap);
+      KV2[1] = laplace_val2(T2[1], LO2[1], ltab, T.lap);
+    } else if constexpr (KT == KS_GAUSS_UNSCALED) {
+      const uint64_t S2h = pk2(T.s2, T.s2), S2l = pk2(T.s2l, T.s2l);
+      KV2[0] = exp2_prod2(T2[0], LO2[0], S2h, S2l);
+      KV2[1] = exp2_prod2(T2[1], LO2[1], S2h, S2l);
+    } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
+      // factor h_i h_j (negative) as a float pair, two columns at a time
+      const uint64_t AH = pk2(am.h, am.h), AHL = pk2(__int_as_float(am.pad[1]), __int_as_float(am.pad[1]));
+#pragma unroll
+      for (int p2 = 0; p2 < 2; p2++) {
+        const uint64_t HC = pk2(f4(hh, 2 * p2), f4(hh, 2 * p2 + 1)), HL = pk2(f4(hl, 2 * p2), f4(hl, 2 * p2 + 1));
+        const uint64_t PH = mul2(AH, HC);
+        const uint64_t PL = add2(fma2(AH, HC, sub2(0, PH)), fma2(AH, HL, mul2(AHL, HC)));
+        KV2[p2] = exp2_prod2(T2[p2], LO2[p2], PH, PL);
+      }
+    }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       const int j = j4 + q;
@@ -906,15 +960,9 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
       const float lo = (q & 1) ? hi2(LO2[q >> 1]) : lo2(LO2[q >> 1]);
       const float s = (q & 1) ? hi2(S2[q >> 1]) : lo2(S2[q >> 1]);
       float kv;
-      if constexpr (KT == KS_LAPLACE) kv = laplace_val(t, lo, ltab, T.lap);
-      else if constexpr (KT == KS_GAUSS_UNSCALED) kv = exp2_prod(t, lo, T.s2, T.s2l);
-      else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
-        // factor h_i h_j (negative) as a float pair
-        const float hc = f4(hh, q);
-        const float ph = am.h * hc;
-        const float pl = fmaf(am.h, hc, -ph) + fmaf(am.h, f4(hl, q), __int_as_float(am.pad[1]) * hc);
-        kv = exp2_prod(t, lo, ph, pl);
-      } else kv = kval32<KT>(t, lo, 0.f, am.h, 0.f, kp);
+      if constexpr (KT == KS_LAPLACE || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH)
+        kv = (q & 1) ? hi2(KV2[q >> 1]) : lo2(KV2[q >> 1]);
+      else kv = kval32<KT>(t, lo, 0.f, am.h, 0.f, kp);
       if constexpr (FLAGS) {
         if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
           const float f = -am.h * f4(hh, q);      // 0.5 log2(e) h_i h_j
@@ -1022,28 +1070,30 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   double rchk = 0.0;
   float fchk = 0.f;                 // |rechecked values|, for the underflow test
   bool nchk = false;
+  // columns per TMEM load: 8 for the kernels with the most live state per column
+  constexpr int NCH = (KT == KS_LAPLACE || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH) ? 8 : 16;
 #pragma unroll 1
-  for (int half = 0; half < 2; half++) {
-    const int c0 = grp * 32 + half * 16;
-    uint32_t h[16], l[16];
-    tmem_ld16(tH + c0, h);
-    tmem_ld16(tH + 128 + c0, l);
+  for (int part = 0; part < 32 / NCH; part++) {
+    const int c0 = grp * 32 + part * NCH;
+    uint32_t h[NCH], l[NCH];
+    tmem_ld<NCH>(tH + c0, h);
+    tmem_ld<NCH>(tH + 128 + c0, l);
     tmem_ld_wait();
-    if (dump) dump_chunk<KT, 16>(a.dump, row, c0, h, l, bm, am, rc, T.kp);
+    if (dump) dump_chunk<KT, NCH>(a.dump, row, c0, h, l, bm, am, rc, T.kp);
     if constexpr (KT == KS_GAUSSIAN) {
-      if (gfast) { epi_chunk_gfast<16>(h, l, bm, c0, am.n_hi, rc, acc); continue; }
+      if (gfast) { epi_chunk_gfast<NCH>(h, l, bm, c0, am.n_hi, rc, acc); continue; }
     }
     if constexpr (kt_uses_norms(KT)) {
       uint32_t flags = 0;
       const bool fl = T.any_flag != 0;
       if (exact) {
-        if (fl) flags = epi_chunk<KT, true, true, 16>(h, l, bm, c0, am, rc, T, ltab, acc);
-        else epi_chunk<KT, true, false, 16>(h, l, bm, c0, am, rc, T, ltab, acc);
+        if (fl) flags = epi_chunk<KT, true, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc);
+        else epi_chunk<KT, true, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc);
       } else {
-        if (fl) flags = epi_chunk<KT, false, true, 16>(h, l, bm, c0, am, rc, T, ltab, acc);
-        else epi_chunk<KT, false, false, 16>(h, l, bm, c0, am, rc, T, ltab, acc);
+        if (fl) flags = epi_chunk<KT, false, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc);
+        else epi_chunk<KT, false, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc);
       }
-      // FP64 rechecks of the flagged pairs of these 16 columns
+      // rechecks of the flagged pairs of these columns
       while (flags) {
         const int j = __ffs(flags) - 1;
         flags &= flags - 1;
@@ -1056,7 +1106,7 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
         }
       }
     } else {
-      epi_chunk_ip<KT, 16>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      epi_chunk_ip<KT, NCH>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
     }
   }
   const float fs = (acc[0] + acc[1]) + (acc[2] + acc[3]);
@@ -1114,6 +1164,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
   }
   if (warp == 0) { tmem_alloc(&S->tmem_base, TMEM_COLS); tmem_relinquish(); }
   if constexpr (KT == KS_LAPLACE || KT == KS_LIST) laplace_table(S->ltab);
+
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
