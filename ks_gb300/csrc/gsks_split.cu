@@ -66,6 +66,7 @@ constexpr int BN = 128;             // sources per tile
 constexpr int KPAD_MAX = 64;        // padded k of the target-resident kernel
 constexpr int NSTAGE = 3;           // source-tile operand stages
 constexpr int LTAB = 256;           // Laplace log2 table entries
+constexpr size_t SMEM_MAX = 232448; // dynamic shared memory per block (227 KB)
 constexpr int NMETA = 4;            // source-tile metadata ring
 constexpr int NBLK = 3;             // slices per operand
 constexpr int EPI_GROUPS = 4;          // column groups of the epilogue
@@ -179,8 +180,16 @@ struct SmemLayout {
   size_t chunk_al;     // chunk_op rounded up to 1 KiB
   size_t stage_bytes;  // one stage: the source chunk, or both operands' chunks
   size_t a_region;     // target image (resident) or target metadata
+  int tab_sh;          // Laplace table: log2 of its copies (0 or 3), -1 without table
 };
-__host__ __device__ inline SmemLayout smem_layout(int kpad)
+__host__ __device__ inline size_t smem_fixed(const SmemLayout &L);
+
+// kt: the kernel selector (the Laplace table is sized for KS_LAPLACE and KS_LIST).
+// The table is replicated eight times when it fits, one copy per bank group of
+// a quarter warp, so that table lookups never conflict; the resident Laplace
+// form then keeps two source stages instead of three (its epilogue, not the
+// copies, sets the pace).
+__host__ __device__ inline SmemLayout smem_layout(int kpad, int kt)
 {
   SmemLayout L;
   L.kc = kchunk(kpad);
@@ -188,10 +197,16 @@ __host__ __device__ inline SmemLayout smem_layout(int kpad)
   L.resident = (L.nch == 1);
   L.chunk_op = (size_t)NBLK * BM * L.kc * 2;
   L.chunk_al = (L.chunk_op + 1023) & ~(size_t)1023;
-  L.nstage = L.resident ? NSTAGE : 2;
+  const bool tab = kt == KS_LAPLACE || kt == KS_LIST;
+  L.nstage = L.resident ? (tab ? 2 : NSTAGE) : 2;
   L.stage_bytes = L.resident ? L.chunk_al : 2 * L.chunk_al;
   L.a_region = L.resident ? ((tile_bytes(BM, kpad) + 1023) & ~(size_t)1023)
                           : (((size_t)BM * sizeof(PtMeta) + 1023) & ~(size_t)1023);
+  L.tab_sh = -1;
+  if (tab) {
+    L.tab_sh = 3;
+    if (smem_fixed(L) + ((size_t)LTAB << 3) * 16 > SMEM_MAX) L.tab_sh = 0;
+  }
   return L;
 }
 
@@ -571,9 +586,16 @@ struct SplitSmem {
   int abort;
   int never;             // stays 0: an abort flag for the drain waits
   double rsum[2][EPI_GROUPS - 1][BM];   // row sums of epilogue groups 1.., by item parity
-  float4 ltab[LTAB];     // Laplace log2 table
   TaskParam tslot[2];    // list form: the current items' task parameters, by item parity
 };
+
+
+// Shared memory without the Laplace table (which follows SplitSmem).
+__host__ __device__ inline size_t smem_fixed(const SmemLayout &L)
+{
+  return 1024 /* alignment slack */ + L.a_region + L.nstage * L.stage_bytes + NMETA * (size_t)BN * sizeof(PtMeta) +
+         sizeof(SplitSmem) + 64;
+}
 
 template <int KT>
 __device__ __forceinline__ const TaskParam &pick_task(const TaskParam &slot, const TaskParam &single)
@@ -587,16 +609,25 @@ __device__ __forceinline__ const TaskParam &pick_task(const TaskParam &slot, con
 // significant bits (so that r = f c_i - 1 is exact up to one rounding of a
 // value below 2^-8.8), and -log2(c_i) as an integer on the 2^-12 grid (bits in
 // .z) plus an FP32 remainder (.y).  Filled once per CTA in FP64.
-__device__ void laplace_table(float4 *tab)
+// Entry i sits at tab[(i << sh) + g] for each of the 2^sh copies g.
+__device__ void laplace_table(float4 *tab, int sh)
 {
   for (int i = threadIdx.x; i < LTAB; i += blockDim.x) {
     const double fm = 1.0 + (i + 0.5) / LTAB;
     const double c = rint(4096.0 / fm) / 4096.0;
     const double T = -log2(c);
     const double th = rint(T * 4096.0);
-    tab[i] = make_float4((float)c, (float)(T - th / 4096.0), __int_as_float((int)th), 0.f);
+    const float4 v = make_float4((float)c, (float)(T - th / 4096.0), __int_as_float((int)th), 0.f);
+    for (int g = 0; g < (1 << sh); g++) tab[(i << sh) + g] = v;
   }
 }
+
+// A thread's view of the table: its copy and the copies' stride.
+struct LTab {
+  const float4 *p;      // tab + this lane's copy
+  int sh;
+  __device__ __forceinline__ float4 operator[](uint32_t i) const { return p[i << sh]; }
+};
 
 // scal * d2^powe for the double-float d2 = t + lo, powe = -P/2, as
 // 2^(log2 scal + powe log2 d2).  log2 d2 = e + (-log2 c_i) + log2(1 + r) +
@@ -605,7 +636,7 @@ __device__ void laplace_table(float4 *tab)
 // 2^-13-grid parts are formed exactly in int32, the rest in FP32, so that the
 // result carries a relative error of a few 1e-7 for every P up to 1022.
 // Values below 2^-126 flush to zero (rows of such values are redone in FP64).
-__device__ __forceinline__ float laplace_core(float t, float lo, const float4 *__restrict__ tab, const LapParam &L,
+__device__ __forceinline__ float laplace_core(float t, float lo, const LTab &tab, const LapParam &L,
                                               int &n)
 {
   const uint32_t u = __float_as_uint(t);
@@ -621,7 +652,7 @@ __device__ __forceinline__ float laplace_core(float t, float lo, const float4 *_
   n = E >> 13;
   return ex2_approx(arg);
 }
-__device__ __forceinline__ float laplace_val(float t, float lo, const float4 *__restrict__ tab, const LapParam &L)
+__device__ __forceinline__ float laplace_val(float t, float lo, const LTab &tab, const LapParam &L)
 {
   int n;
   const float y = laplace_core(t, lo, tab, L, n);
@@ -629,8 +660,7 @@ __device__ __forceinline__ float laplace_val(float t, float lo, const float4 *__
 }
 
 // laplace_val of two columns, the floating-point part in packed FP32 pairs.
-__device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const float4 *__restrict__ tab,
-                                                 const LapParam &L)
+__device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const LTab &tab, const LapParam &L)
 {
   const float t0 = lo2(T), t1 = hi2(T);
   const uint32_t u0 = __float_as_uint(t0), u1 = __float_as_uint(t1);
@@ -780,7 +810,7 @@ __device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb
 // and overflowing Laplace pairs, the other kernels and the single-call form go
 // through FP64.
 template <int KT>
-__device__ double recheck(const TileArgs &a, const TaskParam &T, const float4 *ltab, int ipos, int jpos)
+__device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &ltab, int ipos, int jpos)
 {
   int pa = a.amap ? a.amap[ipos] : ipos;
   int pb = a.bmap ? a.bmap[jpos] : jpos;
@@ -911,7 +941,7 @@ __device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const u
 template <int KT, bool EXACT, bool FLAGS, int NC>
 __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                               const SrcMeta *__restrict__ bm, int c0, const PtMeta &am, float rc,
-                                              const TaskParam &T, const float4 *__restrict__ ltab,
+                                              const TaskParam &T, const LTab &ltab,
                                               float (&acc)[4])
 {
   const KParams &kp = T.kp;
@@ -1064,7 +1094,7 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 template <int KT>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
                                               const SrcMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
-                                              bool gfast, bool dump, const float4 *ltab, double &racc)
+                                              bool gfast, bool dump, const LTab &ltab, double &racc)
 {
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   double rchk = 0.0;
@@ -1136,7 +1166,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *sm = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int kpad = a.kpad;
-  const SmemLayout L = smem_layout(kpad);
+  const SmemLayout L = smem_layout(kpad, KT);
   const bool resident = L.resident;
   const size_t a_bytes = tile_bytes(BM, kpad), b_bytes = tile_bytes(BN, kpad);
   const size_t a_op = NBLK * blk_bytes(BM, kpad);     // operand part of a tile image
@@ -1163,7 +1193,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     fence_mbar_init();
   }
   if (warp == 0) { tmem_alloc(&S->tmem_base, TMEM_COLS); tmem_relinquish(); }
-  if constexpr (KT == KS_LAPLACE || KT == KS_LIST) laplace_table(S->ltab);
+  float4 *tab_base = (float4 *)((uint8_t *)S + ((sizeof(SplitSmem) + 15) & ~(size_t)15));
+  if constexpr (KT == KS_LAPLACE || KT == KS_LIST) laplace_table(tab_base, L.tab_sh);
 
   tc_fence_before();
   __syncthreads();
@@ -1283,6 +1314,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     // sub-partition, in two 16-column TMEM loads.
     const int ew = warp - 2;
     const int grp = ew >> 2;
+    const LTab ltab{tab_base + (L.tab_sh > 0 ? (lane & ((1 << L.tab_sh) - 1)) : 0), L.tab_sh > 0 ? L.tab_sh : 0};
     const int qd = warp & 3;
     const int row = qd * 32 + lane;
     const Params *P = a.P;
@@ -1315,24 +1347,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         if constexpr (KT == KS_LIST) {
           switch (T.kp.type) {
             case KS_GAUSSIAN:
-              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
+              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
             case KS_POLYNOMIAL:
-              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
+              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
+              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
             case KS_TANH:
-              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
+              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
             case KS_QUARTIC:
-              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
+              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
             case KS_MULTIQUADRATIC:
-              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
+              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
             default:
-              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, S->ltab, racc); break;
+              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
           }
         } else {
-          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, S->ltab, racc);
+          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, ltab, racc);
         }
         tc_fence_before();
         __syncwarp();
@@ -1398,11 +1430,10 @@ cudaError_t launch_tiles(const TileArgs &a, int grid, size_t smem, cudaStream_t 
   }
 }
 
-size_t smem_bytes(int kpad)
+size_t smem_bytes(int kpad, int kt)
 {
-  const SmemLayout L = smem_layout(kpad);
-  return 1024 /* alignment slack */ + L.a_region + L.nstage * L.stage_bytes + NMETA * (size_t)BN * sizeof(PtMeta) +
-         sizeof(SplitSmem) + 64;
+  const SmemLayout L = smem_layout(kpad, kt);
+  return smem_fixed(L) + (L.tab_sh >= 0 ? ((size_t)LTAB << L.tab_sh) * 16 : 0);
 }
 
 }  // namespace split
@@ -1488,7 +1519,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
     cudaMemcpyAsync((uint8_t *)tl_split_params + 64, centre, (size_t)k * 8, cudaMemcpyDeviceToDevice, s);
   }
   const int grid = std::min(ntm * nsc, sms);
-  cudaError_t e = launch_tiles(a, grid, smem_bytes(kpad), s);
+  cudaError_t e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
   if (e == cudaSuccess) {
     split_reduce<<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, u, umap);
     e = cudaGetLastError();
@@ -1638,7 +1669,7 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
   a.tp = tp;
   a.btile_cols = (const int *)(ws + o_tbc);
   const int grid = std::min((int)items.size(), sms);
-  cudaError_t e = launch_tiles(a, grid, smem_bytes(kpad), s);
+  cudaError_t e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
   if (e != cudaSuccess) return cuda_status(e, "split list launch");
   *launches += 7;
   return GSKS_OK;
