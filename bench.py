@@ -38,6 +38,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -85,6 +86,9 @@ def parse():
     ap.add_argument("--n", type=int, default=N_S)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--no-list", action="store_true", help="skip the batched (dgsks_list) section")
+    ap.add_argument("--config", default=None, choices=["c3", "c5a", "c5b"],
+                    help="one of the other benchmark configurations instead of the default line: c3 (mixture, "
+                         "k swept), c5a (variable bandwidth, 2^20 points), c5b (k = 1024 polynomial)")
     return ap.parse_args()
 
 
@@ -665,10 +669,161 @@ def run_reference(args, ws, rank):
             "e2e": {"value": v, "unit": "pair-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ---------------------------------------------------------------------------
+# The other configurations of the benchmark specification, each at full size:
+# the split form timed over all pairs; the FP64 form timed on a block of target
+# rows (its throughput does not depend on m once every SM is busy); errors of
+# both on sampled rows against the oracle.
+CONFIG_SPECS = {
+    "c3": dict(desc="split vs FP64: m=n=131072 points of a 64-component Gaussian mixture (centres U[-10,10]^k, "
+                    "sigma 0.05, 1% exact duplicates), targets = sources; Gaussian h=0.2 and polynomial pwr 2",
+               m=131072, ks=[3, 8, 32, 128, 512]),
+    "c5a": dict(desc="variable-bandwidth Gaussian: m=n=2^20 points uniform[0,1]^8, per-point bandwidth h "
+                     "log-uniform in [0.01, 0.5], hi = hj = 1/h (K = exp(-d2 / (2 h_i h_j)))",
+                m=1 << 20, ks=[8]),
+    "c5b": dict(desc="dense: m=n=262144 points N(0, 1/k), k=1024, polynomial pwr 4 (scal 1, cons 1)",
+                m=262144, ks=[1024]),
+}
+
+
+def _config_data(torch, name, k, m, seed):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    extra = {}
+    if name == "c3":
+        cent = (torch.rand(64, k, dtype=torch.float64, device="cuda", generator=g) * 20.0 - 10.0)
+        lab = torch.randint(0, 64, (m,), device="cuda", generator=g)
+        X = cent[lab] + 0.05 * torch.randn(m, k, dtype=torch.float64, device="cuda", generator=g)
+        nd = m // 100
+        src = torch.randperm(m, device="cuda", generator=g)[:nd]
+        dst = torch.randperm(m, device="cuda", generator=g)[:nd]
+        X[dst] = X[src]
+        kernels = [("gaussian", 0, dict(scal=-12.5)), ("polynomial", 1, dict(scal=1.0 / k, cons=1.0, powe=2.0))]
+    elif name == "c5a":
+        X = torch.rand(m, k, dtype=torch.float64, device="cuda", generator=g)
+        h = torch.exp(torch.rand(m, dtype=torch.float64, device="cuda", generator=g) * (math.log(0.5) - math.log(0.01))
+                      + math.log(0.01))
+        extra["hinv"] = (1.0 / h).contiguous()
+        kernels = [("varbw", 3, {})]
+    else:
+        X = torch.randn(m, k, dtype=torch.float64, device="cuda", generator=g) / math.sqrt(k)
+        kernels = [("polynomial", 1, dict(scal=1.0, cons=1.0, powe=4.0))]
+    w = torch.randn(m, dtype=torch.float64, device="cuda", generator=g)
+    return X.contiguous(), w, kernels, extra
+
+
+def run_config(args):
+    import numpy as np
+    import torch
+    from ks_gb300 import build as B
+    if not os.path.exists(B.LIB):
+        B.build()
+    from ks_gb300 import gsks
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    spec = CONFIG_SPECS[args.config]
+    m = spec["m"]
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    peaks = peaks_file()
+    tc_peak = peaks.get("bf16_tflops", 1900.0) * 1e12
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    results = []
+    clk = ClockSampler(0)
+    for k in spec["ks"]:
+        X, w, kernels, extra = _config_data(torch, args.config, k, m, 1000 + k)
+        X2 = torch.empty(m, dtype=torch.float64, device="cuda")
+        gsks.norms_device(X, X2, stream=stream)
+        ident = torch.arange(m, dtype=torch.int32, device="cuda")
+        for name, kt, p in kernels:
+            kp = dict(p)
+            if "hinv" in extra:
+                kp.update(hi=extra["hinv"], hj=extra["hinv"])
+            ker = gsks.make_kernel(kt, **kp)
+
+            def call(u, rows, prec):
+                mm = rows.numel()
+                gsks.dgsks_device(ker, mm, m, k, u, rows, X, X2, rows, X, X2, ident, w, ident, precision=prec,
+                                  stream=stream, nxa=m, nxb=m)
+
+            # split over all pairs
+            u = torch.zeros(m, dtype=torch.float64, device="cuda")
+            for _ in range(max(1, args.warmup)):
+                call(u, ident, gsks.GSKS_SPLIT_BF16X3)
+            u.zero_()
+            torch.cuda.synchronize()
+            ts = []
+            with clk:
+                for _ in range(args.steps):
+                    flush.zero_()
+                    a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    call(u, ident, gsks.GSKS_SPLIT_BF16X3)
+                    b.record(stream)
+                    torch.cuda.synchronize()
+                    ts.append(a.elapsed_time(b))
+            t_split = statistics.median(ts) * 1e-3
+            pairs = float(m) * m
+            u_split = (u / args.steps).cpu().numpy()
+            # FP64 on a block of rows sized to about half a second
+            est = 1.06e12 / (2 * k + 40)
+            mr = int(min(m, max(152 * 2 * 64, est * 0.5 / m)))
+            mr = (mr // 64) * 64
+            rows = torch.randperm(m, device="cuda")[:mr].to(torch.int32).sort().values
+            uf = torch.zeros(m, dtype=torch.float64, device="cuda")
+            call(uf, rows[:64], gsks.GSKS_FP64)
+            uf.zero_()
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            call(uf, rows, gsks.GSKS_FP64)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t_fp64 = a.elapsed_time(b) * 1e-3
+            fp64_rate = float(mr) * m / t_fp64
+            # errors on sampled rows of the FP64 block
+            hrows = rows.cpu().numpy()
+            rng = np.random.default_rng(k)
+            sample = np.sort(rng.choice(hrows, min(256, hrows.size), replace=False)).astype(np.int32)
+            Xh = X.cpu().numpy()
+            X2h = O.norms(Xh)
+            wh = w.cpu().numpy()
+            okp = dict(p)
+            if "hinv" in extra:
+                hh = extra["hinv"].cpu().numpy()
+                okp.update(hi=hh, hj=hh)
+            idh = np.arange(m, dtype=np.int32)
+            ref, cond = O.rows(O.make_kernel(kt, **okp), sample, Xh, X2h, idh, Xh, X2h, idh, wh, idh)
+            ufh = uf.cpu().numpy()
+            err = {"split": {kk: float("%.3g" % v) for kk, v in O.errors(u_split[sample], ref, cond=cond).items()},
+                   "fp64": {kk: float("%.3g" % v) for kk, v in O.errors(ufh[sample], ref, cond=cond).items()}}
+            alg = 2.0 * pairs * k
+            results.append({"k": k, "kernel": name, "pairs": pairs,
+                            "split": {"value": pairs / t_split, "ms": round(t_split * 1e3, 3),
+                                      "alg_tflops": round(alg / t_split / 1e12, 2),
+                                      "frac_alg_tensor": round(alg / tc_peak / t_split, 4)},
+                            "fp64": {"value": fp64_rate, "rows_timed": mr, "ms": round(t_fp64 * 1e3, 2)},
+                            "split_over_fp64": (pairs / t_split) / fp64_rate,
+                            "error": err, "rows_checked": int(sample.size)})
+            del u, uf
+        del X, X2, w, ident
+        torch.cuda.empty_cache()
+    line = {"metric": METRIC, "unit": "pair-evals/s", "config": {"workload": spec["desc"], "name": args.config},
+            "steps": args.steps, "warmup": args.warmup, "data": "synthetic, seeded (torch generator on the device)",
+            "timing": "split: CUDA events per call over all m*n pairs, median of the timed steps, L2 flushed "
+                      "before each; fp64: one call over a block of target rows x all sources",
+            "results": results, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.case:
         run_case(args)
+        return
+    if args.config:
+        run_config(args)
         return
     if args.impl == "reference":
         ws = int(os.environ.get("WORLD_SIZE", "1")); rank = int(os.environ.get("RANK", "0"))

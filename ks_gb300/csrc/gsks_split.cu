@@ -403,9 +403,11 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   out[t] = T;
 }
 
-// Float-pair copy of a pool: Xf[i] = (hi, lo), hi + lo = X[i] to 2^-48.
-__global__ void pool_split(long long n, const double *__restrict__ X, float2 *__restrict__ Xf)
+// Float-pair copy of a pool: Xf[i] = (hi, lo), hi + lo = X[i] to 2^-48.  With
+// P != nullptr (a single call) only when the call may flag pairs.
+__global__ void pool_split(long long n, const double *__restrict__ X, float2 *__restrict__ Xf, const Params *P)
 {
+  if (P && !P->any_flag) return;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)blockDim.x * gridDim.x) {
     const double v = X[i];
     const float h = (float)v;
@@ -683,7 +685,8 @@ __device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const 
   return mul2(pk2(ex2_approx(lo2(ARG)), ex2_approx(hi2(ARG))), pk2(s0, s1));
 }
 
-// 2^n y in FP64, n in the FP64 exponent range (beyond it, 0 or inf).
+// 2^n y in FP64, n in the normal FP64 exponent range (beyond it, 0 or inf;
+// the rechecks send results below the normal range through FP64).
 __device__ __forceinline__ double scale2(float y, int n)
 {
   if (n < -1022) return 0.0;
@@ -714,11 +717,14 @@ __device__ __forceinline__ uint64_t exp2_prod2(uint64_t T, uint64_t LO, uint64_t
 // 2^((t + lo)(ph + pl)) as exp2_prod, returned in FP64 so that values below
 // the FP32 range keep their size (the integer part of the exponent is applied
 // in FP64).
-__device__ __forceinline__ double exp2_prod_wide(float t, float lo, float ph, float pl)
+__device__ __forceinline__ double exp2_prod_wide(float t, float lo, float ph, float pl, bool &deep)
 {
   const float a = t * ph;
   const float ae = fmaf(t, ph, -a) + fmaf(lo, ph, t * pl);
   const float n = floorf(a);
+  // results in the FP64 subnormal band go through FP64; below it FP64 gives 0 too
+  deep = n < -1020.0f && n > -1090.0f;
+  if (n <= -1090.0f) return 0.0;
   const float f = (a - n) + ae;                  // a - n is exact
   const float e = ex2_approx(f);
   return scale2(e, (int)n);
@@ -816,8 +822,10 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
   int pb = a.bmap ? a.bmap[jpos] : jpos;
   if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
   if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
-  if constexpr (KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH || KT == KS_LAPLACE) {
-    if (a.XAf && a.P->ff_ok) {
+  if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH ||
+                KT == KS_LAPLACE) {
+    if (a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag)) {   // the copies exist
+      // (a single call builds them only when it may flag pairs)
       const float2 *x = a.XAf + (size_t)pa * a.k, *y = a.XBf + (size_t)pb * a.k;
       float sh = 0.f, sl = 0.f;
       for (int p = 0; p < a.k; p++) {
@@ -836,17 +844,21 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
       }
       const float th = sh + sl, tl = sl - (th - sh);
       const double wv = a.w[a.wmap ? a.wmap[jpos] : jpos];
-      if constexpr (KT == KS_GAUSS_UNSCALED) {
-        return exp2_prod_wide(th, tl, T.s2, T.s2l) * wv;
+      bool deep = false;
+      if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED) {
+        const double v = exp2_prod_wide(th, tl, T.s2, T.s2l, deep) * wv;
+        if (!deep) return v;
       } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
         const double f = -0.5 * 1.4426950408889634 * T.kp.hi[pa] * T.kp.hj[pb];
         const float fh = (float)f, fl = (float)(f - (double)fh);
-        return exp2_prod_wide(th, tl, fh, fl) * wv;
+        const double v = exp2_prod_wide(th, tl, fh, fl, deep) * wv;
+        if (!deep) return v;
       } else {
         if (th > T.lap.tover && th >= 1e-15f) {
           int n;
           const float y = laplace_core(th, tl, ltab, T.lap, n);
-          return scale2(y, n) * wv;
+          if (n >= -1020) return scale2(y, n) * wv;
+          if (n <= -1090) return 0.0;
         }
       }
     }
@@ -1322,7 +1334,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     const bool exact = P->exact_t1 != 0, gfast = P->gfast != 0;
     TaskParam T0;                                  // the single call's parameters
     if constexpr (KT != KS_LIST) {
-      T0.kp = a.kp; T0.t_flag = P->t_flag; T0.rho = P->rho; T0.s2 = T0.s2l = 0.f;
+      const double s2 = a.kp.scal * 1.4426950408889634;   // Gaussian rechecks from pool coordinates
+      T0.kp = a.kp; T0.t_flag = P->t_flag; T0.rho = P->rho;
+      T0.s2 = (float)s2; T0.s2l = (float)(s2 - (double)T0.s2);
       T0.lap = P->lap; T0.any_flag = P->any_flag; T0.centred = P->centred;
     }
     int g = 0, tc = 0;
@@ -1469,7 +1483,14 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const size_t o_a = o_bbox + al((size_t)2 * k * 8);
   const size_t o_b = o_a + al((size_t)ntm * tile_bytes(BM, kpad));
   const size_t o_p = o_b + al((size_t)ntn * tile_bytes(BN, kpad));
-  const size_t total = o_p + al((size_t)nsc * ldp * 8);
+  // float-pair copies of the pools for cheap rechecks, when the pools are known
+  // and not much larger than the gathered points
+  const bool same_pool = XA == XB && nxa == nxb;
+  const long long pool_pts = nxa < 0 || nxb < 0 ? -1 : (long long)nxa + (same_pool ? 0 : nxb);
+  const bool ff = kt_rescue(ker->type) && pool_pts >= 0 && pool_pts <= std::max(4LL * (m + n), 1LL << 22);
+  const size_t o_xaf = o_p + al((size_t)nsc * ldp * 8);
+  const size_t o_xbf = o_xaf + (ff ? al((size_t)nxa * k * sizeof(float2)) : 0);
+  const size_t total = o_xbf + (ff && !same_pool ? al((size_t)nxb * k * sizeof(float2)) : 0);
   uint8_t *ws = nullptr;
   if (stream_ordered_alloc) {
     cudaError_t e = cudaMallocAsync((void **)&ws, total, s);
@@ -1507,6 +1528,14 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   a.XA = XA; a.XB = XB; a.amap = amap; a.bmap = bmap; a.wmap = wmap; a.w = w;
   a.nxa = nxa; a.nxb = nxb;
   a.hi = hi; a.hj = hj;
+  if (ff) {
+    float2 *xaf = (float2 *)(ws + o_xaf), *xbf = same_pool ? xaf : (float2 *)(ws + o_xbf);
+    const long long na_c = (long long)nxa * k, nb_c = (long long)nxb * k;
+    pool_split<<<(int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1), 256, 0, s>>>(na_c, XA, xaf, P);
+    if (!same_pool)
+      pool_split<<<(int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1), 256, 0, s>>>(nb_c, XB, xbf, P);
+    a.XAf = xaf; a.XBf = xbf;
+  }
   a.kp = make_kparams(ker, hi, hj);
   a.kp.coinc = coincidence_eps(k);
   a.P = P;
@@ -1651,9 +1680,9 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
   float2 *xaf = (float2 *)(ws + o_xaf), *xbf = same_pool ? xaf : (float2 *)(ws + o_xbf);
   {
     const long long na_c = (long long)nxa * k, nb_c = (long long)nxb * k;
-    pool_split<<<(int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1), 256, 0, s>>>(na_c, XA, xaf);
+    pool_split<<<(int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1), 256, 0, s>>>(na_c, XA, xaf, nullptr);
     if (!same_pool)
-      pool_split<<<(int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1), 256, 0, s>>>(nb_c, XB, xbf);
+      pool_split<<<(int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1), 256, 0, s>>>(nb_c, XB, xbf, nullptr);
   }
   TileArgs a{};
   a.k = k; a.kpad = kpad; a.kt = KS_LIST;
