@@ -815,7 +815,7 @@ __device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb
 // instructions issue too slowly on this GPU to recheck many pairs.  Coincident
 // and overflowing Laplace pairs, the other kernels and the single-call form go
 // through FP64.
-template <int KT>
+template <int KT, bool PRE = false>
 __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &ltab, int ipos, int jpos)
 {
   int pa = a.amap ? a.amap[ipos] : ipos;
@@ -827,6 +827,15 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
     if (a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag)) {   // the copies exist
       // (a single call builds them only when it may flag pairs)
       const float2 *x = a.XAf + (size_t)pa * a.k, *y = a.XBf + (size_t)pb * a.k;
+      double hf = 0.0;
+      if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) hf = T.kp.hi[pa] * T.kp.hj[pb];
+      if constexpr (PRE && KT != KS_LAPLACE) {
+        // an FP32 estimate first: exponents beyond -1100 are 0 in FP64 as well
+        float e2 = 0.f;
+        for (int p = 0; p < a.k; p++) { const float d = x[p].x - y[p].x; e2 = fmaf(d, d, e2); }
+        const float fexp = KT == KS_GAUSSIAN_VAR_BANDWIDTH ? (float)(0.7213475204444817 * hf) : -T.s2;
+        if (e2 * fexp > 1111.0f) return 0.0;
+      }
       float sh = 0.f, sl = 0.f;
       for (int p = 0; p < a.k; p++) {
         const float2 u = x[p], v = y[p];
@@ -849,7 +858,7 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
         const double v = exp2_prod_wide(th, tl, T.s2, T.s2l, deep) * wv;
         if (!deep) return v;
       } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
-        const double f = -0.5 * 1.4426950408889634 * T.kp.hi[pa] * T.kp.hj[pb];
+        const double f = -0.5 * 1.4426950408889634 * hf;
         const float fh = (float)f, fl = (float)(f - (double)fh);
         const double v = exp2_prod_wide(th, tl, fh, fl, deep) * wv;
         if (!deep) return v;
@@ -954,7 +963,7 @@ template <int KT, bool EXACT, bool FLAGS, int NC>
 __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                               const SrcMeta *__restrict__ bm, int c0, const PtMeta &am, float rc,
                                               const TaskParam &T, const LTab &ltab,
-                                              float (&acc)[4])
+                                              float (&acc)[4], float &amin)
 {
   const KParams &kp = T.kp;
   uint32_t flags = 0;
@@ -1005,6 +1014,11 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
       if constexpr (KT == KS_LAPLACE || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH)
         kv = (q & 1) ? hi2(KV2[q >> 1]) : lo2(KV2[q >> 1]);
       else kv = kval32<KT>(t, lo, 0.f, am.h, 0.f, kp);
+      // smallest exponent (log2 units) of the exponential kernels' values: the
+      // row rescue is needed only if some value is not 0 in FP64 either
+      if constexpr (KT == KS_GAUSSIAN) amin = fminf(amin, t);
+      else if constexpr (KT == KS_GAUSS_UNSCALED) amin = fminf(amin, -T.s2 * t);
+      else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) amin = fminf(amin, -am.h * f4(hh, q) * t);
       if constexpr (FLAGS) {
         if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
           const float f = -am.h * f4(hh, q);      // 0.5 log2(e) h_i h_j
@@ -1112,6 +1126,7 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   double rchk = 0.0;
   float fchk = 0.f;                 // |rechecked values|, for the underflow test
   bool nchk = false;
+  float amin = gfast ? 0.f : 3.0e38f;   // see epi_chunk (not tracked by the Gaussian fast path)
   // columns per TMEM load: 8 for the kernels with the most live state per column
   constexpr int NCH = (KT == KS_LAPLACE || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH) ? 8 : 16;
 #pragma unroll 1
@@ -1129,11 +1144,11 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
       uint32_t flags = 0;
       const bool fl = T.any_flag != 0;
       if (exact) {
-        if (fl) flags = epi_chunk<KT, true, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc);
-        else epi_chunk<KT, true, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc);
+        if (fl) flags = epi_chunk<KT, true, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        else epi_chunk<KT, true, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
       } else {
-        if (fl) flags = epi_chunk<KT, false, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc);
-        else epi_chunk<KT, false, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc);
+        if (fl) flags = epi_chunk<KT, false, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        else epi_chunk<KT, false, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
       }
       // rechecks of the flagged pairs of these columns
       while (flags) {
@@ -1157,10 +1172,10 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     // (FP32 flushes values below 2^-126 to zero, FP64 keeps them down to
     // 2^-1074) takes these pairs from FP64 instead, flagged pairs included.
     const float W = bm->wsum[grp * 32];
-    if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W) {
+    if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W && (KT == KS_LAPLACE || amin < 1111.0f)) {
       double r = 0.0;
       const int c1 = min(grp * 32 + 32, ncols);
-      for (int c = grp * 32; c < c1; c++) r += recheck<KT>(a, T, ltab, am.pos, bm->pos[c]);
+      for (int c = grp * 32; c < c1; c++) r += recheck<KT, true>(a, T, ltab, am.pos, bm->pos[c]);
       if constexpr (KT == KS_GAUSSIAN) {
         if (gfast) r /= (double)am.h;   // the caller applies the row factor to the row sum
       }
