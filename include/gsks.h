@@ -151,6 +151,30 @@ int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
                double *XB, double *XB2, int nxb,
                double *w, int nw);
 
+/* ---- planned batched evaluation ----------------------------------------- */
+/* A plan fixes the task lists, kernel descriptors, sizes and precision of a
+ * dgsks_list and keeps their work tables (tile / item queues, the owner lists
+ * of u, workspace) on the device.  gsks_list_plan_execute then evaluates it
+ * for device-resident coordinates, norms (NULL: computed on the device),
+ * weights and u, asynchronously on `stream` (a cudaStream_t).  The first
+ * execute captures the evaluation into a CUDA graph; later executes with the
+ * same pointers and stream replay the graph.  Lists given as device arrays and
+ * device bandwidth arrays must stay valid while the plan exists (host arrays
+ * are copied at creation).  same_pool != 0: executes pass XB == XA.  The
+ * reference has no counterpart (its list driver plans on every call,
+ * frame/omp_dgsks_list.cpp:297-359). */
+typedef struct gsks_list_plan gsks_list_plan;
+int gsks_list_plan_create(gsks_list_plan **plan, ks_t *kernel, ks_t *kernels, int ntask, int k, int nu,
+                          const int *a_off, const int *a_idx, const int *u_idx,
+                          const int *b_off, const int *b_idx, const int *w_idx,
+                          int nxa, int nxb, int nw, int precision, int same_pool);
+int gsks_list_plan_execute(gsks_list_plan *plan, double *u, const double *XA, const double *XA2,
+                           const double *XB, const double *XB2, const double *w, void *stream);
+/* Waits for the device, then returns and clears the plan's device-side error
+ * flags (as gsks_device_errors); -1 if they could not be read. */
+int gsks_list_plan_errors(gsks_list_plan *plan);
+int gsks_list_plan_destroy(gsks_list_plan *plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,15 +73,24 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k,
                   const double *w, const int *wmap, const double *hi, const double *hj,
                   cudaStream_t s, bool stream_ordered_alloc);
 
-// Split-precision form of dgsks_list (gsks_split.cu): row sums of every
-// (task t, target position r, source chunk sc) into
-// partial[pbase[t] + sc * m_t + r], chunk sources per chunk (a multiple of
-// 128).  kps: ntask device-side descriptors; hoff_a / hoff_b: host offsets;
-// everything else device pointers.  Adds its launch count to *launches.
-int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
-                       const long long *pbase, int chunk, const double *XA, const int *a_idx, int nxa,
-                       const double *XB, const int *b_idx, int nxb, const double *w, const int *w_idx,
-                       double *partial, cudaStream_t s, int *launches);
+// Split-precision form of dgsks_list (gsks_split.cu), planned once for a set
+// of lists: row sums of every (task t, target position r, source chunk sc)
+// into partial[pbase[t] + sc * m_t + r], chunk sources per chunk (a multiple
+// of 128).  kps: ntask device-side descriptors; hoff_a / hoff_b: host
+// offsets.  split_list_run takes device pointers and only launches kernels.
+struct SplitListPlan {
+  int ntask = 0, k = 0, kpad = 0, ma = 0, mb = 0, nxa = 0, nxb = 0;
+  int n_ta = 0, n_tb = 0, n_items = 0;
+  bool same_pool = false;
+  DevBuf ws;
+  size_t o_params = 0, o_centre = 0, o_bbox = 0, o_ta = 0, o_tat = 0, o_tb = 0, o_tbt = 0, o_tbc = 0;
+  size_t o_items = 0, o_kps = 0, o_tp = 0, o_a = 0, o_b = 0, o_xaf = 0, o_xbf = 0;
+};
+int split_list_plan(SplitListPlan &P, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
+                    const long long *pbase, int chunk, int nxa, int nxb, bool same_pool, cudaStream_t s);
+int split_list_run(const SplitListPlan &P, Ctx *c, const double *XA, const int *a_idx, const double *XB,
+                   const int *b_idx, const double *w, const int *w_idx, double *partial, int *err, cudaStream_t s,
+                   int *launches);
 
 // Owner lists of the batched merge (gsks_sort.cu): u_idx holds na device
 // indices in [0, nu) (others raise DEVERR_MAP_RANGE in *err).  Writes own_pos

@@ -1582,10 +1582,12 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
 // partial[pbase[t] + sc * m_t + r], the layout the list merge reads.  One
 // bounding box, hence one scale and one centre, covers all tasks, and the
 // per-task flag thresholds come from it.
-int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
-                       const long long *pbase, int chunk, const double *XA, const int *a_idx, int nxa,
-                       const double *XB, const int *b_idx, int nxb, const double *w, const int *w_idx,
-                       double *partial, cudaStream_t s, int *launches)
+//
+// split_list_plan builds the tile and item tables of a fixed set of lists on
+// the device (and sizes the workspace); split_list_run evaluates them with the
+// current coordinates and weights, launches only.
+int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
+                    const long long *pbase, int chunk, int nxa, int nxb, bool same_pool, cudaStream_t s)
 {
   using namespace split;
   if (chunk % BN) return GSKS_ERR_ARG;
@@ -1611,8 +1613,8 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
       tb_cols.push_back(std::min(BN, n - j0));
     }
     const int ntn = (int)tb.size() - b_base;
-    // relative epilogue cost per tile: the Laplace powering dominates
-    const double wkt = kps[t].type == KS_LAPLACE ? 4.0 : 1.0;
+    // relative epilogue cost per tile: the Laplace evaluation dominates
+    const double wkt = kps[t].type == KS_LAPLACE ? 3.0 : 1.0;
     for (int sc = 0; sc * chunk_tiles < ntn; sc++)
       for (int i0 = 0; i0 < m; i0 += BM) {
         SplitItem it{};
@@ -1626,7 +1628,6 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
         cost.push_back(wkt * (it.b1 - it.b0));
       }
   }
-  if (items.empty()) return GSKS_OK;
   {
     std::vector<int> ord(items.size());
     for (size_t i = 0; i < ord.size(); i++) ord[i] = (int)i;
@@ -1638,84 +1639,100 @@ int enqueue_split_list(Ctx *c, const KParams *kps, int ntask, int k, const int *
   if (na > INT32_MAX || nb > INT32_MAX) return GSKS_ERR_TOO_LARGE;
 
   auto al = [](size_t x) { return (x + 1023) & ~(size_t)1023; };
-  const size_t o_params = 0;
-  const size_t o_centre = al(sizeof(Params));
-  const size_t o_bbox = o_centre + al((size_t)k * 8);
-  const size_t o_ta = o_bbox + al((size_t)2 * k * 8);
-  const size_t o_tat = o_ta + al(ta.size() * sizeof(int2));
-  const size_t o_tb = o_tat + al(ta.size() * sizeof(int));
-  const size_t o_tbt = o_tb + al(tb.size() * sizeof(int2));
-  const size_t o_tbc = o_tbt + al(tb.size() * sizeof(int));
-  const size_t o_items = o_tbc + al(tb.size() * sizeof(int));
-  const size_t o_kps = o_items + al(items.size() * sizeof(SplitItem));
-  const size_t o_tp = o_kps + al((size_t)ntask * sizeof(KParams));
-  const size_t o_a = o_tp + al((size_t)ntask * sizeof(TaskParam));
-  const size_t o_b = o_a + al(ta.size() * tile_bytes(BM, kpad));
+  Pl.ntask = ntask; Pl.k = k; Pl.kpad = kpad;
+  Pl.ma = hoff_a[ntask]; Pl.mb = hoff_b[ntask];
+  Pl.nxa = nxa; Pl.nxb = nxb; Pl.same_pool = same_pool;
+  Pl.n_ta = (int)ta.size(); Pl.n_tb = (int)tb.size(); Pl.n_items = (int)items.size();
+  Pl.o_params = 0;
+  Pl.o_centre = al(sizeof(Params));
+  Pl.o_bbox = Pl.o_centre + al((size_t)k * 8);
+  Pl.o_ta = Pl.o_bbox + al((size_t)2 * k * 8);
+  Pl.o_tat = Pl.o_ta + al(ta.size() * sizeof(int2));
+  Pl.o_tb = Pl.o_tat + al(ta.size() * sizeof(int));
+  Pl.o_tbt = Pl.o_tb + al(tb.size() * sizeof(int2));
+  Pl.o_tbc = Pl.o_tbt + al(tb.size() * sizeof(int));
+  Pl.o_items = Pl.o_tbc + al(tb.size() * sizeof(int));
+  Pl.o_kps = Pl.o_items + al(items.size() * sizeof(SplitItem));
+  Pl.o_tp = Pl.o_kps + al((size_t)ntask * sizeof(KParams));
+  Pl.o_a = Pl.o_tp + al((size_t)ntask * sizeof(TaskParam));
+  Pl.o_b = Pl.o_a + al(ta.size() * tile_bytes(BM, kpad));
   // float-pair copies of the pools for the rechecks (one when both sides share it)
-  const bool same_pool = XA == XB && nxa == nxb;
-  const size_t o_xaf = o_b + al(tb.size() * tile_bytes(BN, kpad));
-  const size_t o_xbf = o_xaf + al((size_t)nxa * k * sizeof(float2));
-  const size_t total = o_xbf + (same_pool ? 0 : al((size_t)nxb * k * sizeof(float2)));
-  if (!c->dwork.ensure(total)) return GSKS_ERR_ALLOC;
-  uint8_t *ws = (uint8_t *)c->dwork.p;
-  Params *P = (Params *)(ws + o_params);
-  double *centre = (double *)(ws + o_centre);
-  long long *bbox = (long long *)(ws + o_bbox);
-  TaskParam *tp = (TaskParam *)(ws + o_tp);
+  Pl.o_xaf = Pl.o_b + al(tb.size() * tile_bytes(BN, kpad));
+  Pl.o_xbf = Pl.o_xaf + al((size_t)nxa * k * sizeof(float2));
+  const size_t total = Pl.o_xbf + (same_pool ? 0 : al((size_t)nxb * k * sizeof(float2)));
+  if (!Pl.ws.ensure(total)) return GSKS_ERR_ALLOC;
+  uint8_t *ws = (uint8_t *)Pl.ws.p;
   auto up = [&](size_t off, const void *src, size_t bytes) {
     return bytes == 0 || cudaMemcpyAsync(ws + off, src, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
   };
-  if (!(up(o_ta, ta.data(), ta.size() * sizeof(int2)) && up(o_tat, ta_task.data(), ta_task.size() * sizeof(int)) &&
-        up(o_tb, tb.data(), tb.size() * sizeof(int2)) && up(o_tbt, tb_task.data(), tb_task.size() * sizeof(int)) &&
-        up(o_tbc, tb_cols.data(), tb_cols.size() * sizeof(int)) &&
-        up(o_items, items.data(), items.size() * sizeof(SplitItem)) &&
-        up(o_kps, kps, (size_t)ntask * sizeof(KParams))))
+  if (!(up(Pl.o_ta, ta.data(), ta.size() * sizeof(int2)) &&
+        up(Pl.o_tat, ta_task.data(), ta_task.size() * sizeof(int)) &&
+        up(Pl.o_tb, tb.data(), tb.size() * sizeof(int2)) &&
+        up(Pl.o_tbt, tb_task.data(), tb_task.size() * sizeof(int)) &&
+        up(Pl.o_tbc, tb_cols.data(), tb_cols.size() * sizeof(int)) &&
+        up(Pl.o_items, items.data(), items.size() * sizeof(SplitItem)) &&
+        up(Pl.o_kps, kps, (size_t)ntask * sizeof(KParams))))
     return cuda_status(cudaGetLastError(), "split list tables");
+  // the host vectors above die here: the copies must have left them
+  cudaError_t e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? GSKS_OK : cuda_status(e, "split list tables");
+}
 
+int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int *a_idx, const double *XB,
+                   const int *b_idx, const double *w, const int *w_idx, double *partial, int *err, cudaStream_t s,
+                   int *launches)
+{
+  using namespace split;
+  if (Pl.n_items == 0) return GSKS_OK;
+  const int k = Pl.k, kpad = Pl.kpad, ntask = Pl.ntask, nxa = Pl.nxa, nxb = Pl.nxb;
+  uint8_t *ws = (uint8_t *)Pl.ws.p;
+  Params *P = (Params *)(ws + Pl.o_params);
+  double *centre = (double *)(ws + Pl.o_centre);
+  long long *bbox = (long long *)(ws + Pl.o_bbox);
+  TaskParam *tp = (TaskParam *)(ws + Pl.o_tp);
   const float tau = 5e-7f;
   const int sms = std::max(1, c->num_sms);
-  int *err = (int *)c->err.p;
   bbox_init<<<1, 256, 0, s>>>(k, bbox);
   {
     // every list position (tasks with an empty side included: harmless)
-    const int ma = hoff_a[ntask], mb = hoff_b[ntask];
-    const long long tot = ((long long)ma + mb) * k;
+    const long long tot = ((long long)Pl.ma + Pl.mb) * k;
     const int blocks = (int)std::max<long long>((k + 255) / 256,
                                                 std::min<long long>(8LL * sms, std::max<long long>(1, (tot + 255) / 256)));
-    bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(ma, mb, k, XA, a_idx, nxa, XB, b_idx, nxb, err, bbox);
+    bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(Pl.ma, Pl.mb, k, XA, a_idx, nxa, XB, b_idx, nxb, err,
+                                                               bbox);
   }
   params_kernel<<<1, 1024, 0, s>>>(k, KS_LIST, 0.0, 0.0, tau, bbox, centre, P);
-  task_params_kernel<<<(ntask + 127) / 128, 128, 0, s>>>(ntask, (const KParams *)(ws + o_kps), P, tau, tp);
-  pack_kernel<<<(int)ta.size(), BM, 0, s>>>(0, 0, k, kpad, XA, a_idx, nxa, err, nullptr, nullptr, nullptr, KS_LIST,
-                                            centre, P, ws + o_a, (const int2 *)(ws + o_ta),
-                                            (const int *)(ws + o_tat), tp);
-  pack_kernel<<<(int)tb.size(), BN, 0, s>>>(1, 0, k, kpad, XB, b_idx, nxb, err, w, w_idx, nullptr, KS_LIST,
-                                            centre, P, ws + o_b, (const int2 *)(ws + o_tb),
-                                            (const int *)(ws + o_tbt), tp);
-  float2 *xaf = (float2 *)(ws + o_xaf), *xbf = same_pool ? xaf : (float2 *)(ws + o_xbf);
+  task_params_kernel<<<(ntask + 127) / 128, 128, 0, s>>>(ntask, (const KParams *)(ws + Pl.o_kps), P, tau, tp);
+  pack_kernel<<<Pl.n_ta, BM, 0, s>>>(0, 0, k, kpad, XA, a_idx, nxa, err, nullptr, nullptr, nullptr, KS_LIST,
+                                     centre, P, ws + Pl.o_a, (const int2 *)(ws + Pl.o_ta),
+                                     (const int *)(ws + Pl.o_tat), tp);
+  pack_kernel<<<Pl.n_tb, BN, 0, s>>>(1, 0, k, kpad, XB, b_idx, nxb, err, w, w_idx, nullptr, KS_LIST,
+                                     centre, P, ws + Pl.o_b, (const int2 *)(ws + Pl.o_tb),
+                                     (const int *)(ws + Pl.o_tbt), tp);
+  float2 *xaf = (float2 *)(ws + Pl.o_xaf), *xbf = Pl.same_pool ? xaf : (float2 *)(ws + Pl.o_xbf);
   {
     const long long na_c = (long long)nxa * k, nb_c = (long long)nxb * k;
     pool_split<<<(int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1), 256, 0, s>>>(na_c, XA, xaf, nullptr);
-    if (!same_pool)
+    if (!Pl.same_pool)
       pool_split<<<(int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1), 256, 0, s>>>(nb_c, XB, xbf, nullptr);
   }
   TileArgs a{};
   a.k = k; a.kpad = kpad; a.kt = KS_LIST;
   a.XAf = xaf; a.XBf = xbf;
-  a.imgA = ws + o_a; a.imgB = ws + o_b;
+  a.imgA = ws + Pl.o_a; a.imgB = ws + Pl.o_b;
   a.XA = XA; a.XB = XB; a.amap = a_idx; a.bmap = b_idx; a.wmap = w_idx; a.w = w;
   a.nxa = nxa; a.nxb = nxb;
   a.P = P;
   a.partial = partial;
   a.err = err;
-  a.tab = (const SplitItem *)(ws + o_items);
-  a.ntab = (int)items.size();
+  a.tab = (const SplitItem *)(ws + Pl.o_items);
+  a.ntab = Pl.n_items;
   a.tp = tp;
-  a.btile_cols = (const int *)(ws + o_tbc);
-  const int grid = std::min((int)items.size(), sms);
+  a.btile_cols = (const int *)(ws + Pl.o_tbc);
+  const int grid = std::min(Pl.n_items, sms);
   cudaError_t e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
   if (e != cudaSuccess) return cuda_status(e, "split list launch");
-  *launches += 7;
+  *launches += Pl.same_pool ? 8 : 9;
   return GSKS_OK;
 }
 

@@ -76,6 +76,15 @@ def load():
     lib.ks_malloc_aligned.argtypes = [ip, ip, ip]
     if hasattr(lib, "dgsks_list"):
         lib.dgsks_list.restype = C.c_int
+    lib.gsks_list_plan_create.restype = C.c_int
+    lib.gsks_list_plan_create.argtypes = [C.POINTER(vp), C.POINTER(KsT), vp, ip, ip, ip, vp, vp, vp, vp, vp, vp,
+                                          ip, ip, ip, ip, ip]
+    lib.gsks_list_plan_execute.restype = C.c_int
+    lib.gsks_list_plan_execute.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.gsks_list_plan_errors.restype = C.c_int
+    lib.gsks_list_plan_errors.argtypes = [vp]
+    lib.gsks_list_plan_destroy.restype = C.c_int
+    lib.gsks_list_plan_destroy.argtypes = [vp]
     _lib = lib
     return lib
 
@@ -197,6 +206,48 @@ def dgsks_list(ker: KsT, u, a_off, a_idx, b_off, b_idx, XA, XA2, XB, XB2, w,
                         _vp(XB), _vp(XB2), C.c_int(int(XB.shape[0])), _vp(w), C.c_int(nw))
     if rc:
         raise GsksError(rc, "dgsks_list")
+
+
+class ListPlan:
+    """A planned dgsks_list (gsks.h gsks_list_plan_*): the lists, kernels and
+    precision are fixed at construction; execute() evaluates for device
+    tensors u, XA, XB, w (norms optional) and replays a CUDA graph when called
+    again with the same tensors and stream.  Device lists must outlive the plan."""
+
+    def __init__(self, ker: KsT, a_off, a_idx, b_off, b_idx, k: int, nu: int, nxa: int, nxb: int, nw: int,
+                 u_idx=None, w_idx=None, kers=None, precision=GSKS_FP64, same_pool=False):
+        lib = load()
+        ntask = int((a_off.numel() if hasattr(a_off, "numel") else a_off.size) - 1)
+        self._kers = (KsT * ntask)(*kers) if kers is not None else None
+        self._keep = (ker, a_off, a_idx, b_off, b_idx, u_idx, w_idx, kers)
+        h = C.c_void_p()
+        rc = lib.gsks_list_plan_create(C.byref(h), C.byref(ker), C.cast(self._kers, C.c_void_p) if self._kers else None,
+                                       ntask, int(k), int(nu), _vp(a_off), _vp(a_idx), _vp(u_idx), _vp(b_off),
+                                       _vp(b_idx), _vp(w_idx), int(nxa), int(nxb), int(nw), int(precision),
+                                       1 if same_pool else 0)
+        if rc:
+            raise GsksError(rc, "gsks_list_plan_create")
+        self._h = h
+
+    def execute(self, u, XA, XA2, XB, XB2, w, stream=None) -> None:
+        s = None if stream is None else C.c_void_p(stream.cuda_stream)
+        rc = load().gsks_list_plan_execute(self._h, _vp(u), _vp(XA), _vp(XA2), _vp(XB), _vp(XB2), _vp(w), s)
+        if rc:
+            raise GsksError(rc, "gsks_list_plan_execute")
+
+    def errors(self) -> int:
+        return int(load().gsks_list_plan_errors(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load().gsks_list_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------
