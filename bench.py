@@ -479,9 +479,29 @@ def run_list(args, torch, gsks, forms):
         dt = time.perf_counter() - t0
         out[form] = {"value": L["pairs"] * args.steps / dt, "unit": "pair-evals/s",
                      "ms_per_step": dt * 1e3 / args.steps, "gpu_launches": gsks.last_launch_count()}
+        # the same lists planned once: every step replays the captured CUDA graph
+        plan = gsks.ListPlan(kers[0], d_lists["a_off"], d_lists["a_idx"], d_lists["b_off"], d_lists["b_idx"],
+                             LIST_K, LIST_POOL, LIST_POOL, LIST_POOL, LIST_POOL, kers=kers,
+                             precision=prec_of(gsks, form), same_pool=True)
+        stream = torch.cuda.current_stream()
+        for _ in range(max(1, args.warmup)):
+            plan.execute(u, X, None, X, None, w, stream=stream)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True); ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.execute(u, X, None, X, None, w, stream=stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        pt = ev0.elapsed_time(ev1) * 1e-3
+        out[form]["planned"] = {"value": L["pairs"] * args.steps / pt, "ms_per_step": pt * 1e3 / args.steps,
+                                "timing": "CUDA events around graph replays of gsks_list_plan_execute"}
+        assert plan.errors() == 0
+        plan.close()
     gsks.set_precision(gsks.GSKS_FP64)
     if "split" in out and "fp64" in out:
         out["split_over_fp64"] = out["split"]["value"] / out["fp64"]["value"]
+        out["split_over_fp64_planned"] = out["split"]["planned"]["value"] / out["fp64"]["planned"]["value"]
 
     # errors on a subset of tasks
     rng = np.random.default_rng(17)
