@@ -544,6 +544,7 @@ struct TileArgs {
   KParams kp;                       // FP64 descriptor for the rechecks
   const Params *P;
   double *partial;                  // [nsc][ldp]
+  float *pskip;                     // [nsc][ldp]: W sums of the groups left to the row rescue (single calls)
   int ldp;
   int *err;
   float *dump;                      // test hook: H, L, t, lo, K of CTA 0's first tile
@@ -588,6 +589,7 @@ struct SplitSmem {
   int abort;
   int never;             // stays 0: an abort flag for the drain waits
   double rsum[2][EPI_GROUPS - 1][BM];   // row sums of epilogue groups 1.., by item parity
+  float rskip[2][EPI_GROUPS - 1][BM];   // their skipped-group weights (pskip)
   TaskParam tslot[2];    // list form: the current items' task parameters, by item parity
 };
 
@@ -1114,13 +1116,17 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 
 // One warp's share of one tile (32 columns of its 32 rows): TMEM loads, kernel
 // values, weighted sums, FP64 rechecks of the flagged pairs.  Adds the row
-// sum of these columns to racc.  The 32 columns are summed in FP32 (four
+// sum of these columns to racc.  Where every value of the 32 columns lies
+// below 2^-96, a single call (a.pskip set) adds the columns' sum of |w| to bsk
+// and leaves the decision to split_reduce, which sees the whole row; the list
+// form rescues the columns at once.  The 32 columns are summed in FP32 (four
 // interleaved partial sums) and enter the FP64 row sum with one conversion and
 // one add: FP64 instructions issue at a small fraction of the FP32 rate here.
 template <int KT>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
                                               const SrcMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
-                                              bool gfast, bool dump, const LTab &ltab, double &racc)
+                                              bool gfast, bool dump, const LTab &ltab, double &racc,
+                                              float &bsk)
 {
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   double rchk = 0.0;
@@ -1173,6 +1179,14 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     // 2^-1074) takes these pairs from FP64 instead, flagged pairs included.
     const float W = bm->wsum[grp * 32];
     if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W && (KT == KS_LAPLACE || amin < 1111.0f)) {
+      if (a.pskip) {
+        // these columns add less than 2^-96 W to the row: whether that matters
+        // depends on the rest of the row (split_reduce)
+        bsk += W;
+        racc += (double)fs;
+        if (nchk) racc += rchk;
+        return;
+      }
       double r = 0.0;
       const int c1 = min(grp * 32 + 32, ncols);
       for (int c = grp * 32; c < c1; c++) r += recheck<KT, true>(a, T, ltab, am.pos, bm->pos[c]);
@@ -1363,6 +1377,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->a_empty);
       double racc = 0.0;
+      float bsk = 0.0f;
       bool ok = true;
       for (int tj = G.t0; tj < G.t1; tj++, g++, tc++) {
         const int ms = g % NMETA, buf = tc & 1;
@@ -1376,24 +1391,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         if constexpr (KT == KS_LIST) {
           switch (T.kp.type) {
             case KS_GAUSSIAN:
-              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
+              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
             case KS_POLYNOMIAL:
-              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
+              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
+              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
             case KS_TANH:
-              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
+              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
             case KS_QUARTIC:
-              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
+              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
             case KS_MULTIQUADRATIC:
-              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
+              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
             default:
-              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc); break;
+              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
           }
         } else {
-          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, ltab, racc);
+          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, ltab, racc, bsk);
         }
         tc_fence_before();
         __syncwarp();
@@ -1402,12 +1417,19 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       if (!ok) break;
       // combine the groups' row sums in group order (double-buffered by item parity)
       double (*xs)[BM] = S->rsum[it & 1];
-      if (grp > 0) xs[grp - 1][row] = racc;
+      float (*xb)[BM] = S->rskip[it & 1];
+      if (grp > 0) { xs[grp - 1][row] = racc; xb[grp - 1][row] = bsk; }
       asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");
       if (grp == 0) {
-        for (int q = 0; q < EPI_GROUPS - 1; q++) racc += xs[q][row];
-        if (KT == KS_GAUSSIAN && gfast) racc *= (double)am.h;   // the row's low-norm factor
-        if (row < G.rows) a.partial[G.out + row] = racc;
+        for (int q = 0; q < EPI_GROUPS - 1; q++) { racc += xs[q][row]; bsk += xb[q][row]; }
+        if (KT == KS_GAUSSIAN && gfast) {         // the row's low-norm factor
+          racc *= (double)am.h;
+          bsk *= am.h;
+        }
+        if (row < G.rows) {
+          a.partial[G.out + row] = racc;
+          if (a.pskip) a.pskip[G.out + row] = bsk;
+        }
       }
     }
   }
@@ -1418,14 +1440,72 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
 }
 
 // u[umap[i]] += sum over chunks of the chunk partials, in chunk order.
-__global__ void split_reduce(int m, int nsc, int ldp, const double *__restrict__ partial, double *__restrict__ u,
-                             const int *__restrict__ umap)
+// Groups of columns whose values all lay below 2^-96 were left out of the row
+// sums (pskip holds their sums of |w|, b): their part of row i is below
+// 2^-96 b.  Where that could reach 2^-27 of |s| (in practice: rows whose
+// every value is that small) the row goes to the rescue list instead.
+__global__ void split_reduce(int m, int nsc, int ldp, const double *__restrict__ partial,
+                             const float *__restrict__ pskip, double *__restrict__ u, const int *__restrict__ umap,
+                             int *__restrict__ rlist, int *__restrict__ rcount)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   double s = 0.0;
+  float b = 0.0f;
   for (int c = 0; c < nsc; c++) s += partial[(size_t)c * ldp + i];
+  if (pskip) {
+    for (int c = 0; c < nsc; c++) b += pskip[(size_t)c * ldp + i];
+    if (b > 0.0f && fabs(s) < 0x1p-69 * (double)b) {
+      rlist[atomicAdd(rcount, 1)] = i;
+      return;
+    }
+  }
   u[umap ? umap[i] : i] += s;
+}
+
+// The rows of the rescue list, one warp per row: every pair of the row from
+// the pool coordinates (recheck: float-pair distances, values in the FP64
+// range), summed in FP64 in a fixed order.
+template <int KT>
+__global__ void __launch_bounds__(256) split_rescue(TileArgs a, const int *__restrict__ rlist,
+                                                    const int *__restrict__ rcount, double *__restrict__ u,
+                                                    const int *__restrict__ umap)
+{
+  __shared__ float4 tab[LTAB];
+  if constexpr (KT == KS_LAPLACE) laplace_table(tab, 0);
+  __syncthreads();
+  const LTab ltab{tab, 0};
+  const Params *P = a.P;
+  TaskParam T;
+  {
+    const double s2 = a.kp.scal * 1.4426950408889634;
+    T.kp = a.kp; T.t_flag = P->t_flag; T.rho = P->rho;
+    T.s2 = (float)s2; T.s2l = (float)(s2 - (double)T.s2);
+    T.lap = P->lap; T.any_flag = P->any_flag; T.centred = P->centred;
+  }
+  const int nr = *rcount, lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < nr; e += nw) {
+    const int i = rlist[e];
+    double r = 0.0;
+    for (int j = lane; j < a.n; j += 32) r += recheck<KT, true>(a, T, ltab, i, j);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (lane == 0) u[umap ? umap[i] : i] += r;
+  }
+}
+
+cudaError_t launch_rescue(const TileArgs &a, int grid, const int *rlist, const int *rcount, double *u,
+                          const int *umap, cudaStream_t s)
+{
+  switch (a.kt) {
+    case KS_GAUSSIAN: split_rescue<KS_GAUSSIAN><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
+    case KS_GAUSSIAN_VAR_BANDWIDTH:
+      split_rescue<KS_GAUSSIAN_VAR_BANDWIDTH><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
+    case KS_LAPLACE: split_rescue<KS_LAPLACE><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
+    default: return cudaSuccess;
+  }
+  return cudaGetLastError();
 }
 
 template <int KT>
@@ -1518,7 +1598,12 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const bool same_pool = XA == XB && nxa == nxb;
   const long long pool_pts = nxa < 0 || nxb < 0 ? -1 : (long long)nxa + (same_pool ? 0 : nxb);
   const bool ff = kt_rescue(ker->type) && pool_pts >= 0 && pool_pts <= std::max(4LL * (m + n), 1LL << 22);
-  const size_t o_xaf = o_p + al((size_t)nsc * ldp * 8);
+  // row rescue (exponential kernels): skipped-group weights, row list, count
+  const bool defer = kt_rescue(ker->type);
+  const size_t o_ps = o_p + al((size_t)nsc * ldp * 8);
+  const size_t o_rl = o_ps + (defer ? al((size_t)nsc * ldp * 4) : 0);
+  const size_t o_rc = o_rl + (defer ? al((size_t)m * 4) : 0);
+  const size_t o_xaf = o_rc + (defer ? al(4) : 0);
   const size_t o_xbf = o_xaf + (ff ? al((size_t)nxa * k * sizeof(float2)) : 0);
   const size_t total = o_xbf + (ff && !same_pool ? al((size_t)nxb * k * sizeof(float2)) : 0);
   uint8_t *ws = nullptr;
@@ -1570,6 +1655,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   a.kp.coinc = coincidence_eps(k);
   a.P = P;
   a.partial = (double *)(ws + o_p);
+  a.pskip = defer ? (float *)(ws + o_ps) : nullptr;
   a.ldp = ldp;
   a.err = (int *)c->err.p;
   a.dump = tl_split_dump;
@@ -1578,14 +1664,17 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
     cudaMemcpyAsync((uint8_t *)tl_split_params + 64, centre, (size_t)k * 8, cudaMemcpyDeviceToDevice, s);
   }
   const int grid = std::min(ntm * nsc, sms);
-  cudaError_t e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
+  int *rlist = defer ? (int *)(ws + o_rl) : nullptr, *rcount = defer ? (int *)(ws + o_rc) : nullptr;
+  cudaError_t e = defer ? cudaMemsetAsync(rcount, 0, sizeof(int), s) : cudaSuccess;
+  if (e == cudaSuccess) e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
   if (e == cudaSuccess) {
-    split_reduce<<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, u, umap);
+    split_reduce<<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, a.pskip, u, umap, rlist, rcount);
     e = cudaGetLastError();
   }
+  if (e == cudaSuccess && defer) e = launch_rescue(a, std::max(1, std::min(2 * sms, (m + 7) / 8)), rlist, rcount, u, umap, s);
   if (stream_ordered_alloc) cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_status(e, "split launch");
-  note_launches(7);
+  note_launches(defer ? 8 : 7);
   return GSKS_OK;
 }
 

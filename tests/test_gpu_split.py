@@ -169,3 +169,25 @@ def test_split_var_bandwidth_narrow(gpu, oracle_mod):
     h = np.exp(rng.uniform(np.log(0.02), np.log(0.7), X.shape[0]))
     e = _run(gpu, oracle_mod, 3, {}, X, w, amap, bmap, umap, wmap, hi=1.0 / h ** 2)
     assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+def test_split_gaussian_rows_partly_below_fp32_range(gpu, oracle_mod):
+    """Sources in two clusters, taken cluster by cluster (so that 32-column
+    groups are pure); targets near either cluster or far from both.  Near rows
+    skip the other cluster's groups (values below the FP32 range, negligible
+    against the row); far rows have only such values and are redone in full."""
+    rng = np.random.default_rng(12)
+    N, k, m, n = 6000, 3, 900, 1200
+    X = np.empty((N, k))
+    X[:2000] = rng.uniform(0.0, 0.1, (2000, k))
+    X[2000:4000] = rng.uniform(0.5, 0.6, (2000, k))
+    X[4000:] = rng.uniform(1.4, 1.5, (2000, k))
+    w = rng.standard_normal(N)
+    bmap = np.concatenate([rng.choice(2000, n // 2, replace=False),
+                           2000 + rng.choice(2000, n // 2, replace=False)]).astype(np.int32)
+    amap = rng.permutation(np.concatenate([rng.choice(2000, m // 3, replace=False) + o
+                                           for o in (0, 2000, 4000)])).astype(np.int32)
+    umap = rng.permutation(N)[:m].astype(np.int32)
+    wmap = rng.permutation(N)[:n].astype(np.int32)
+    e = _run(gpu, oracle_mod, 0, dict(scal=-200.0), X, w, amap, bmap, umap, wmap)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
