@@ -270,6 +270,7 @@ KParams make_kparams(const ks_t *ker, const double *hi, const double *hj)
   const double p = ker->powe;
   if (fabs(p) <= 511.0 && p == rint(p)) { kp.pmode = POW_INT; kp.pint = (int)p; }
   else if (fabs(p) <= 511.0 && 2.0 * p == rint(2.0 * p)) { kp.pmode = POW_HALF; kp.pint = (int)floor(p); }
+  kp.fscal = (float)kp.scal; kp.fcons = (float)kp.cons; kp.fpowe = (float)kp.powe; kp.fpad = 0.0f;
   return kp;
 }
 

@@ -85,6 +85,10 @@ struct SplitListPlan {
   DevBuf ws;
   size_t o_params = 0, o_centre = 0, o_bbox = 0, o_ta = 0, o_tat = 0, o_tb = 0, o_tbt = 0, o_tbc = 0;
   size_t o_items = 0, o_kps = 0, o_tp = 0, o_a = 0, o_b = 0, o_xaf = 0, o_xbf = 0;
+  // deferred row rescue: task geometry, a-list offsets, skipped-group weights
+  // (the partial layout), rescue list and its count
+  size_t o_tg = 0, o_aoff = 0, o_pskip = 0, o_rl = 0, o_rc = 0;
+  size_t o_ni = 0;   // work counter of the tile kernel
 };
 int split_list_plan(SplitListPlan &P, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
                     const long long *pbase, int chunk, int nxa, int nxb, bool same_pool, cudaStream_t s);

@@ -32,6 +32,9 @@ struct KParams {
   // exponents up to 511 in magnitude are evaluated by binary powering (and one
   // square root) instead of the general pow().
   int pmode, pint;
+  // scal, cons, powe rounded to FP32 (the split form's epilogue: FP64
+  // instructions, conversions included, issue slowly on this GPU)
+  float fscal, fcons, fpowe, fpad;
 };
 
 enum { POW_GENERAL = 0, POW_INT = 1, POW_HALF = 2 };

@@ -149,6 +149,14 @@ struct SplitItem {
   int rows, pad;
 };
 
+// One task of the list form as the row rescue sees it: its targets are list
+// positions a0 .. a0 + m - 1, its sources b0 .. b0 + n - 1, and target row r's
+// chunk sums sit at partial[pbase + c * m + r], c < nsc.
+struct SplitTaskGeo {
+  long long pbase;
+  int a0, m, b0, n, nsc, pad;
+};
+
 __host__ __device__ inline size_t blk_bytes(int rows, int kpad) { return (size_t)rows * kpad * 2; }
 __host__ __device__ inline size_t tile_bytes(int rows, int kpad)
 {
@@ -544,7 +552,7 @@ struct TileArgs {
   KParams kp;                       // FP64 descriptor for the rechecks
   const Params *P;
   double *partial;                  // [nsc][ldp]
-  float *pskip;                     // [nsc][ldp]: W sums of the groups left to the row rescue (single calls)
+  float *pskip;                     // W sums of the groups left to the row rescue (the partial layout)
   int ldp;
   int *err;
   float *dump;                      // test hook: H, L, t, lo, K of CTA 0's first tile
@@ -553,6 +561,7 @@ struct TileArgs {
   int ntab;
   const TaskParam *tp;
   const int *btile_cols;            // valid columns of each source tile
+  int *next_item;                   // work counter (zero at launch): items after the first gridDim.x
 };
 
 // Geometry of work item `item`: target tile, source-tile range, task, the
@@ -591,6 +600,7 @@ struct SplitSmem {
   double rsum[2][EPI_GROUPS - 1][BM];   // row sums of epilogue groups 1.., by item parity
   float rskip[2][EPI_GROUPS - 1][BM];   // their skipped-group weights (pskip)
   TaskParam tslot[2];    // list form: the current items' task parameters, by item parity
+  int islot[2];          // the current items (-1: no work left), by item parity
 };
 
 
@@ -754,16 +764,16 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
     const float e = ex2_approx(a);
     return fmaf(e, 0.69314718f * ae, e);
   } else if constexpr (KT == KS_POLYNOMIAL) {
-    const float v = fmaf((float)kp.scal, c, (float)kp.cons);
+    const float v = fmaf(kp.fscal, c, kp.fcons);
     if (kp.pmode == POW_INT) {
       int e = kp.pint < 0 ? -kp.pint : kp.pint;
       float r = 1.0f, b = v;
       for (;;) { if (e & 1) r *= b; e >>= 1; if (!e) break; b *= b; }
       return kp.pint < 0 ? 1.0f / r : r;
     }
-    return ex2_approx((float)kp.powe * __log2f(v));
+    return ex2_approx(kp.fpowe * __log2f(v));
   } else if constexpr (KT == KS_TANH) {
-    const float v = fmaf((float)kp.scal, c, (float)kp.cons);
+    const float v = fmaf(kp.fscal, c, kp.fcons);
     const float av = fabsf(v);
     float r;
     if (av < 0.125f) {
@@ -780,7 +790,7 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
     if (d < 1.0f) { const float u = 1.0f - d; return 0.9375f * u * u; }
     return 0.0f;
   } else if constexpr (KT == KS_MULTIQUADRATIC) {
-    return (t + (float)kp.cons) + lo;
+    return (t + kp.fcons) + lo;
   } else {  // Epanechnikov
     const float d = t + lo;
     return d < 1.0f ? 0.75f * (1.0f - d) : 0.0f;
@@ -808,6 +818,31 @@ __device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb
   else if constexpr (KT == KS_EPANECHNIKOV) kv = d2 < 1.0 ? 0.75 * (1.0 - d2) : 0.0;
   else kv = 0.0;
   return kv * wv;
+}
+
+// Squared distance of two points given as float pairs: TwoSum per coordinate
+// difference, exact square by FMA, TwoSum accumulation (about 2^-44 relative),
+// returned as the float pair th + tl.
+__device__ __forceinline__ void ff_dist2(const float2 *__restrict__ x, const float2 *__restrict__ y, int k,
+                                         float &th, float &tl)
+{
+  float sh = 0.f, sl = 0.f;
+  for (int p = 0; p < k; p++) {
+    const float2 u = x[p], v = y[p];
+    const float s = u.x - v.x;                       // TwoSum(u.x, -v.x)
+    const float bv = s - u.x;
+    float e = (u.x - (s - bv)) + (-v.x - bv);
+    e += u.y - v.y;
+    const float dh = s + e, dl = e - (dh - s);       // Fast2Sum
+    const float q = dh * dh;
+    const float qe = fmaf(dh, dh, -q) + 2.f * dh * dl;
+    const float t = sh + q;                          // TwoSum(sh, q)
+    const float z = t - sh;
+    sl += ((sh - (t - z)) + (q - z)) + qe;
+    sh = t;
+  }
+  th = sh + sl;
+  tl = sl - (th - sh);
 }
 
 // Recheck of one pair.  The list form keeps float-pair copies of the pools:
@@ -838,22 +873,8 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
         const float fexp = KT == KS_GAUSSIAN_VAR_BANDWIDTH ? (float)(0.7213475204444817 * hf) : -T.s2;
         if (e2 * fexp > 1111.0f) return 0.0;
       }
-      float sh = 0.f, sl = 0.f;
-      for (int p = 0; p < a.k; p++) {
-        const float2 u = x[p], v = y[p];
-        const float s = u.x - v.x;                       // TwoSum(u.x, -v.x)
-        const float bv = s - u.x;
-        float e = (u.x - (s - bv)) + (-v.x - bv);
-        e += u.y - v.y;
-        const float dh = s + e, dl = e - (dh - s);       // Fast2Sum
-        const float q = dh * dh;
-        const float qe = fmaf(dh, dh, -q) + 2.f * dh * dl;
-        const float t = sh + q;                          // TwoSum(sh, q)
-        const float z = t - sh;
-        sl += ((sh - (t - z)) + (q - z)) + qe;
-        sh = t;
-      }
-      const float th = sh + sl, tl = sl - (th - sh);
+      float th, tl;
+      ff_dist2(x, y, a.k, th, tl);
       const double wv = a.w[a.wmap ? a.wmap[jpos] : jpos];
       bool deep = false;
       if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED) {
@@ -875,6 +896,34 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
     }
   }
   return recheck64<KT>(a, T.kp, pa, pb, jpos);
+}
+
+// A flagged pair of the Gaussian kinds, FP64-free: the flag rules select pairs
+// whose value lies in the FP32 range, so the value (float-pair distance from
+// the pools' float-pair copies, then exp2_prod) times the column's FP32 weight
+// is formed in FP32 like the main path's.  Needs the copies (ffp).
+template <int KT>
+__device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T, const PtMeta &am,
+                                           const SrcMeta *__restrict__ bm, int c)
+{
+  const int ipos = am.pos, jpos = bm->pos[c];
+  int pa = a.amap ? a.amap[ipos] : ipos;
+  int pb = a.bmap ? a.bmap[jpos] : jpos;
+  if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
+  if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
+  float th, tl;
+  ff_dist2(a.XAf + (size_t)pa * a.k, a.XBf + (size_t)pb * a.k, a.k, th, tl);
+  float ph, pl;
+  if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
+    // (-0.5 log2e hi) hj from the row's and the column's float pairs
+    const float ah = am.h, ahl = __int_as_float(am.pad[1]), hc = bm->h[c], hl = bm->hlo[c];
+    ph = ah * hc;
+    pl = fmaf(ah, hc, -ph) + fmaf(ah, hl, ahl * hc);
+  } else {
+    ph = T.s2;
+    pl = T.s2l;
+  }
+  return exp2_prod(th, tl, ph, pl) * bm->w[c];
 }
 
 // Squared distance t + lo (double-float, scaled units) of one pair from its
@@ -1044,7 +1093,7 @@ __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint
 {
   // two columns per instruction where the kernel allows it (packed FP32 pairs)
   const uint64_t RC = pk2(rc, rc), MH = pk2(-0.5f, -0.5f);
-  const float sc = (float)kp.scal, cn = (float)kp.cons;
+  const float sc = kp.fscal, cn = kp.fcons;
   const uint64_t SC = pk2(sc, sc), CN = pk2(cn, cn);
   const bool ipow = KT == KS_POLYNOMIAL && kp.pmode == POW_INT;
   uint64_t A[2] = {pk2(acc[0], acc[1]), pk2(acc[2], acc[3])};
@@ -1116,10 +1165,8 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 
 // One warp's share of one tile (32 columns of its 32 rows): TMEM loads, kernel
 // values, weighted sums, FP64 rechecks of the flagged pairs.  Adds the row
-// sum of these columns to racc.  Where every value of the 32 columns lies
-// below 2^-96, a single call (a.pskip set) adds the columns' sum of |w| to bsk
-// and leaves the decision to split_reduce, which sees the whole row; the list
-// form rescues the columns at once.  The 32 columns are summed in FP32 (four
+// sum of these columns to racc, and to bsk the columns' sum of |w| where every
+// value of the 32 columns lies below 2^-96.  The 32 columns are summed in FP32 (four
 // interleaved partial sums) and enter the FP64 row sum with one conversion and
 // one add: FP64 instructions issue at a small fraction of the FP32 rate here.
 template <int KT>
@@ -1133,6 +1180,9 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   float fchk = 0.f;                 // |rechecked values|, for the underflow test
   bool nchk = false;
   float amin = gfast ? 0.f : 3.0e38f;   // see epi_chunk (not tracked by the Gaussian fast path)
+  // float-pair copies of the pools exist (a single call builds them only when
+  // it may flag pairs)
+  const bool ffp = a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag);
   // columns per TMEM load: 8 for the kernels with the most live state per column
   constexpr int NCH = (KT == KS_LAPLACE || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH) ? 8 : 16;
 #pragma unroll 1
@@ -1162,6 +1212,14 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
         flags &= flags - 1;
         const int c = c0 + j;
         if (c < ncols && am.pos >= 0) {
+          if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
+            if (ffp) {
+              const float v = recheck_f<KT>(a, T, am, bm, c);
+              acc[0] += v;
+              fchk += fabsf(v);
+              continue;
+            }
+          }
           const double v = recheck<KT>(a, T, ltab, am.pos, bm->pos[c]);
           rchk += v;
           fchk += fabsf((float)v);
@@ -1174,28 +1232,14 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   }
   const float fs = (acc[0] + acc[1]) + (acc[2] + acc[3]);
   if constexpr (kt_rescue(KT)) {
-    // A row whose kernel values over these 32 columns all lie below 2^-96
-    // (FP32 flushes values below 2^-126 to zero, FP64 keeps them down to
-    // 2^-1074) takes these pairs from FP64 instead, flagged pairs included.
+    // Kernel values over these 32 columns all below 2^-96 (FP32 flushes values
+    // below 2^-126 to zero, FP64 keeps them down to 2^-1074): the columns add
+    // less than 2^-96 W to the row, and whether that matters depends on the
+    // rest of the row, summed by other warps and work items.  W goes to bsk;
+    // the reduction redoes the rows where it may matter (split_rescue,
+    // list_rescue).
     const float W = bm->wsum[grp * 32];
-    if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W && (KT == KS_LAPLACE || amin < 1111.0f)) {
-      if (a.pskip) {
-        // these columns add less than 2^-96 W to the row: whether that matters
-        // depends on the rest of the row (split_reduce)
-        bsk += W;
-        racc += (double)fs;
-        if (nchk) racc += rchk;
-        return;
-      }
-      double r = 0.0;
-      const int c1 = min(grp * 32 + 32, ncols);
-      for (int c = grp * 32; c < c1; c++) r += recheck<KT, true>(a, T, ltab, am.pos, bm->pos[c]);
-      if constexpr (KT == KS_GAUSSIAN) {
-        if (gfast) r /= (double)am.h;   // the caller applies the row factor to the row sum
-      }
-      racc += r;
-      return;
-    }
+    if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W && (KT == KS_LAPLACE || amin < 1111.0f)) bsk += W;
   }
   racc += (double)fs;
   if (nchk) racc += rchk;
@@ -1254,9 +1298,20 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       for (int s = 0; s < NSTAGE; s++) b_last[s] = -1;
       for (int s = 0; s < NMETA; s++) m_last[s] = -1;
       bool stop = false;
-      for (int it = 0, item = blockIdx.x; item < items && !*abort && !stop; it++, item += gridDim.x) {
-        const ItemGeo G = item_geo(a, item);
+      // Items are taken from the work counter, so that CTAs with cheap items
+      // take more of them; the item goes to the other roles through islot
+      // (written before the arrive on a_full, which releases it).
+      int item = blockIdx.x;
+      for (int it = 0; !*abort && !stop; it++) {
         if (it > 0 && !mbar_wait(&S->a_empty, (it - 1) & 1, abort, WAIT_LIMIT)) break;
+        if (item >= items) {
+          S->islot[it & 1] = -1;
+          mbar_arrive(&S->a_full);
+          break;
+        }
+        S->islot[it & 1] = item;
+        const int next = atomicAdd(a.next_item, 1) + (int)gridDim.x;   // in flight while this item's copies issue
+        const ItemGeo G = item_geo(a, item);
         const uint8_t *imgA = a.imgA + (size_t)G.ti * a_bytes;
         // slot it & 1 was last read for item it - 2, which every epilogue warp
         // has finished once it arrived on a_empty for item it - 1
@@ -1293,6 +1348,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           bulk_g2s(sBm + ms * meta_bytes, imgB + a_op, (uint32_t)meta_bytes, &S->m_full[ms]);
           m_last[ms] = mu;
         }
+        item = next;
       }
       // On an abort, let the copies already issued land before the CTA exits
       // (each wait bounded; a copy's phase may also have completed long ago).
@@ -1313,9 +1369,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       const uint32_t blk = (uint32_t)BM * L.kc * 2;   // one slice block of one chunk
       int g = 0, tc = 0;
       bool stop = false;
-      for (int it = 0, item = blockIdx.x; item < items && !*abort && !stop; it++, item += gridDim.x) {
-        const ItemGeo G = item_geo(a, item);
+      for (int it = 0; !*abort && !stop; it++) {
         if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
+        const int item = ((volatile int *)S->islot)[it & 1];
+        if (item < 0) break;
+        const ItemGeo G = item_geo(a, item);
         for (int tj = G.t0; tj < G.t1 && !stop; tj++, tc++) {
           const int buf = tc & 1;
           if (tc >= 2 && !mbar_wait(&S->t_empty[buf], ((tc >> 1) - 1) & 1, abort, WAIT_LIMIT)) { stop = true; break; }
@@ -1369,9 +1427,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       T0.lap = P->lap; T0.any_flag = P->any_flag; T0.centred = P->centred;
     }
     int g = 0, tc = 0;
-    for (int it = 0, item = blockIdx.x; item < items && !*abort; it++, item += gridDim.x) {
-      const ItemGeo G = item_geo(a, item);
+    for (int it = 0; !*abort; it++) {
       if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
+      const int item = ((volatile int *)S->islot)[it & 1];
+      if (item < 0) break;
+      const ItemGeo G = item_geo(a, item);
       const TaskParam &T = pick_task<KT>(S->tslot[it & 1], T0);
       const PtMeta am = ((const PtMeta *)sAmeta)[row];
       __syncwarp();
@@ -1603,7 +1663,8 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const size_t o_ps = o_p + al((size_t)nsc * ldp * 8);
   const size_t o_rl = o_ps + (defer ? al((size_t)nsc * ldp * 4) : 0);
   const size_t o_rc = o_rl + (defer ? al((size_t)m * 4) : 0);
-  const size_t o_xaf = o_rc + (defer ? al(4) : 0);
+  const size_t o_ni = o_rc + (defer ? al(4) : 0);   // work counter
+  const size_t o_xaf = o_ni + al(4);
   const size_t o_xbf = o_xaf + (ff ? al((size_t)nxa * k * sizeof(float2)) : 0);
   const size_t total = o_xbf + (ff && !same_pool ? al((size_t)nxb * k * sizeof(float2)) : 0);
   uint8_t *ws = nullptr;
@@ -1656,6 +1717,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   a.P = P;
   a.partial = (double *)(ws + o_p);
   a.pskip = defer ? (float *)(ws + o_ps) : nullptr;
+  a.next_item = (int *)(ws + o_ni);
   a.ldp = ldp;
   a.err = (int *)c->err.p;
   a.dump = tl_split_dump;
@@ -1665,7 +1727,8 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   }
   const int grid = std::min(ntm * nsc, sms);
   int *rlist = defer ? (int *)(ws + o_rl) : nullptr, *rcount = defer ? (int *)(ws + o_rc) : nullptr;
-  cudaError_t e = defer ? cudaMemsetAsync(rcount, 0, sizeof(int), s) : cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(a.next_item, 0, sizeof(int), s);
+  if (e == cudaSuccess && defer) e = cudaMemsetAsync(rcount, 0, sizeof(int), s);
   if (e == cudaSuccess) e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
   if (e == cudaSuccess) {
     split_reduce<<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, a.pskip, u, umap, rlist, rcount);
@@ -1677,6 +1740,75 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   note_launches(defer ? 8 : 7);
   return GSKS_OK;
 }
+
+// ---------------------------------------------------------------------------
+namespace split {
+
+// Deferred row rescue of the list form: a target row of a task whose skipped
+// groups (values below 2^-96) could reach 2^-27 of its sum is listed, then
+// recomputed over all of the task's sources; its chunk sums are replaced by
+// the result (chunk 0) and zeros, so that the merge adds it as before.
+__device__ __forceinline__ int task_of(const int *__restrict__ aoff, int ntask, int pos)
+{
+  int lo = 0, hi = ntask - 1;                    // last t with aoff[t] <= pos
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (aoff[mid] <= pos) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void list_rescue_mark(int ma, int ntask, const int *__restrict__ aoff,
+                                 const SplitTaskGeo *__restrict__ tg, const double *__restrict__ partial,
+                                 const float *__restrict__ pskip, int *__restrict__ rlist, int *__restrict__ rcount)
+{
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ma) return;
+  const SplitTaskGeo G = tg[task_of(aoff, ntask, pos)];
+  const int r = pos - G.a0;
+  double sum = 0.0;
+  float b = 0.0f;
+  for (int c = 0; c < G.nsc; c++) {
+    sum += partial[G.pbase + (long long)c * G.m + r];
+    b += pskip[G.pbase + (long long)c * G.m + r];
+  }
+  if (b > 0.0f && fabs(sum) < 0x1p-69 * (double)b) rlist[atomicAdd(rcount, 1)] = pos;
+}
+
+__global__ void __launch_bounds__(256) list_rescue(TileArgs a, int ntask, const int *__restrict__ aoff,
+                                                   const SplitTaskGeo *__restrict__ tg,
+                                                   const int *__restrict__ rlist, const int *__restrict__ rcount)
+{
+  __shared__ float4 tab[LTAB];
+  laplace_table(tab, 0);
+  __syncthreads();
+  const LTab ltab{tab, 0};
+  const int nr = *rcount, lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < nr; e += nw) {
+    const int pos = rlist[e];
+    const int t = task_of(aoff, ntask, pos);
+    const SplitTaskGeo G = tg[t];
+    const TaskParam &T = a.tp[t];
+    double r = 0.0;
+    for (int j = G.b0 + lane; j < G.b0 + G.n; j += 32) {
+      switch (T.kp.type) {
+        case KS_GAUSSIAN: r += recheck<KS_GAUSS_UNSCALED, true>(a, T, ltab, pos, j); break;
+        case KS_GAUSSIAN_VAR_BANDWIDTH: r += recheck<KS_GAUSSIAN_VAR_BANDWIDTH, true>(a, T, ltab, pos, j); break;
+        default: r += recheck<KS_LAPLACE, true>(a, T, ltab, pos, j); break;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    if (lane == 0) {
+      const int row = pos - G.a0;
+      a.partial[G.pbase + row] = r;
+      for (int c = 1; c < G.nsc; c++) a.partial[G.pbase + (long long)c * G.m + row] = 0.0;
+    }
+  }
+}
+
+}  // namespace split
 
 // ---------------------------------------------------------------------------
 // Split-precision form of dgsks_list.  Every task's targets and sources are
@@ -1741,6 +1873,14 @@ int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, con
     items.swap(sorted);
   }
   if (na > INT32_MAX || nb > INT32_MAX) return GSKS_ERR_TOO_LARGE;
+  std::vector<SplitTaskGeo> tg(ntask);
+  long long ptotal = 0;
+  for (int t = 0; t < ntask; t++) {
+    const int m = hoff_a[t + 1] - hoff_a[t], n = hoff_b[t + 1] - hoff_b[t];
+    const int nsc = (m > 0 && n > 0) ? (n + chunk - 1) / chunk : 0;
+    tg[t] = SplitTaskGeo{pbase[t], hoff_a[t], m, hoff_b[t], n, nsc, 0};
+    ptotal = std::max(ptotal, pbase[t] + (long long)nsc * m);
+  }
 
   auto al = [](size_t x) { return (x + 1023) & ~(size_t)1023; };
   Pl.ntask = ntask; Pl.k = k; Pl.kpad = kpad;
@@ -1761,7 +1901,13 @@ int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, con
   Pl.o_a = Pl.o_tp + al((size_t)ntask * sizeof(TaskParam));
   Pl.o_b = Pl.o_a + al(ta.size() * tile_bytes(BM, kpad));
   // float-pair copies of the pools for the rechecks (one when both sides share it)
-  Pl.o_xaf = Pl.o_b + al(tb.size() * tile_bytes(BN, kpad));
+  Pl.o_tg = Pl.o_b + al(tb.size() * tile_bytes(BN, kpad));
+  Pl.o_aoff = Pl.o_tg + al((size_t)ntask * sizeof(SplitTaskGeo));
+  Pl.o_pskip = Pl.o_aoff + al(((size_t)ntask + 1) * sizeof(int));
+  Pl.o_rl = Pl.o_pskip + al((size_t)std::max(ptotal, 1LL) * sizeof(float));
+  Pl.o_rc = Pl.o_rl + al((size_t)std::max(Pl.ma, 1) * sizeof(int));
+  Pl.o_ni = Pl.o_rc + al(sizeof(int));
+  Pl.o_xaf = Pl.o_ni + al(sizeof(int));
   Pl.o_xbf = Pl.o_xaf + al((size_t)nxa * k * sizeof(float2));
   const size_t total = Pl.o_xbf + (same_pool ? 0 : al((size_t)nxb * k * sizeof(float2)));
   if (!Pl.ws.ensure(total)) return GSKS_ERR_ALLOC;
@@ -1775,7 +1921,9 @@ int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, con
         up(Pl.o_tbt, tb_task.data(), tb_task.size() * sizeof(int)) &&
         up(Pl.o_tbc, tb_cols.data(), tb_cols.size() * sizeof(int)) &&
         up(Pl.o_items, items.data(), items.size() * sizeof(SplitItem)) &&
-        up(Pl.o_kps, kps, (size_t)ntask * sizeof(KParams))))
+        up(Pl.o_kps, kps, (size_t)ntask * sizeof(KParams)) &&
+        up(Pl.o_tg, tg.data(), tg.size() * sizeof(SplitTaskGeo)) &&
+        up(Pl.o_aoff, hoff_a, ((size_t)ntask + 1) * sizeof(int))))
     return cuda_status(cudaGetLastError(), "split list tables");
   // the host vectors above die here: the copies must have left them
   cudaError_t e = cudaStreamSynchronize(s);
@@ -1828,15 +1976,27 @@ int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int 
   a.nxa = nxa; a.nxb = nxb;
   a.P = P;
   a.partial = partial;
+  a.pskip = (float *)(ws + Pl.o_pskip);
+  a.next_item = (int *)(ws + Pl.o_ni);
   a.err = err;
   a.tab = (const SplitItem *)(ws + Pl.o_items);
   a.ntab = Pl.n_items;
   a.tp = tp;
   a.btile_cols = (const int *)(ws + Pl.o_tbc);
   const int grid = std::min(Pl.n_items, sms);
-  cudaError_t e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
+  int *rlist = (int *)(ws + Pl.o_rl), *rcount = (int *)(ws + Pl.o_rc);
+  const SplitTaskGeo *tg = (const SplitTaskGeo *)(ws + Pl.o_tg);
+  const int *aoff = (const int *)(ws + Pl.o_aoff);
+  cudaError_t e = cudaMemsetAsync(rcount, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.next_item, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
+  if (e == cudaSuccess && Pl.ma > 0) {
+    list_rescue_mark<<<(Pl.ma + 255) / 256, 256, 0, s>>>(Pl.ma, ntask, aoff, tg, partial, a.pskip, rlist, rcount);
+    list_rescue<<<std::max(1, std::min(2 * sms, (Pl.ma + 7) / 8)), 256, 0, s>>>(a, ntask, aoff, tg, rlist, rcount);
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess) return cuda_status(e, "split list launch");
-  *launches += Pl.same_pool ? 8 : 9;
+  *launches += Pl.same_pool ? 10 : 11;
   return GSKS_OK;
 }
 
