@@ -121,6 +121,11 @@ struct Params {          // per call, computed on the device
   int ff_ok;             // coordinates within 2^50: float-pair rechecks stay in range
   LapParam lap;          // Laplace exponent constants
   double delta;          // absolute error bound of the assembled d2 (scaled units)
+  // The list form's distance tasks (coordinates taken relative to the centre)
+  // use their own, finer scale; single calls repeat the one above.
+  double sigma_c, inv_sigma_c, q_c, g_c, delta_c;
+  float rc_c;
+  int exact_c;
 };
 
 // Kernel selector of the batched (list) form: the epilogue dispatches on each
@@ -138,6 +143,8 @@ struct __align__(16) TaskParam {
   LapParam lap;          // Laplace
   int any_flag;
   int centred;           // distance kernels: coordinates taken relative to the centre
+  float rc;              // -g of the task's scale (d2 = g (nu_i + nu_j - H - L))
+  int exact;             // nu_i + nu_j - H is exact in FP32 at that scale
 };
 static_assert(sizeof(TaskParam) % 16 == 0, "TaskParam is copied by the bulk-copy engine");
 
@@ -308,27 +315,47 @@ __device__ LapParam lap_param(double scal, double powe)
 __global__ void params_kernel(int k, int kt, double scal, double powe, float tau, const long long *bbox,
                               double *centre, Params *P)
 {
-  __shared__ double s_sq[1024], s_mx[1024];
+  __shared__ double s_sq[1024], s_mx[1024], s_sqc[1024], s_mxc[1024];
   const bool dist = kt_uses_norms(kt);
-  double sq = 0.0, mx = 0.0;
+  double sq = 0.0, mx = 0.0, sqc = 0.0, mxc = 0.0;
   for (int p = threadIdx.x; p < k; p += blockDim.x) {
     const double lo = dval(bbox[p]), hi = dval(bbox[k + p]);
     double c = 0.0, half;
+    const double halfc = 0.5 * (hi - lo);
     if (kt == KS_LIST) { c = 0.5 * (lo + hi); half = fmax(fabs(lo), fabs(hi)); }
-    else if (dist) { c = 0.5 * (lo + hi); half = 0.5 * (hi - lo); }
+    else if (dist) { c = 0.5 * (lo + hi); half = halfc; }
     else half = fmax(fabs(lo), fabs(hi));
     centre[p] = c;
     sq += half * half;
     mx = fmax(mx, half);
+    sqc += halfc * halfc;
+    mxc = fmax(mxc, halfc);
   }
   s_sq[threadIdx.x] = sq; s_mx[threadIdx.x] = mx;
+  s_sqc[threadIdx.x] = sqc; s_mxc[threadIdx.x] = mxc;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {   // fixed-order tree: deterministic
     if ((int)threadIdx.x < s) {
       s_sq[threadIdx.x] += s_sq[threadIdx.x + s];
       s_mx[threadIdx.x] = fmax(s_mx[threadIdx.x], s_mx[threadIdx.x + s]);
+      s_sqc[threadIdx.x] += s_sqc[threadIdx.x + s];
+      s_mxc[threadIdx.x] = fmax(s_mxc[threadIdx.x], s_mxc[threadIdx.x + s]);
     }
     __syncthreads();
+  }
+  if (threadIdx.x == 0 && kt == KS_LIST) {
+    // the centred scale of the list's distance tasks (alpha = 1)
+    const double maxabs = s_mxc[0];
+    double sigma = maxabs > 0.0 ? exp2(ceil(log2(maxabs))) : 1.0;
+    if (sigma < maxabs) sigma *= 2.0;
+    const double nbound = s_sqc[0];
+    const double q = exp2(ceil(log2(2.0 * nbound + 1e-300)) - 23.0);
+    P->sigma_c = sigma; P->inv_sigma_c = 1.0 / sigma; P->q_c = q;
+    P->g_c = 2.0 * sigma * sigma * 0x1p-14;
+    P->rc_c = (float)(-P->g_c);
+    P->delta_c = 2.0 * (sigma * sigma * (double)k * 0x1p-31) +
+                 2.0 * sigma * sqrt((double)k) * sqrt(nbound) * 0x1p-30 + 2.0 * q * 0x1p-23;
+    P->exact_c = (q <= P->g_c) ? 1 : 0;
   }
   if (threadIdx.x == 0) {
     const double log2e = 1.4426950408889634;
@@ -373,6 +400,10 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     // 2 sigma^2 2^-14; when the latter is a multiple of q their sum is exact
     // (it stays below 2^24 q), and only the small L term needs Fast2Sum.
     P->exact_t1 = (q <= 2.0 * sigma * sigma * 0x1p-14) ? 1 : 0;
+    if (kt != KS_LIST) {
+      P->sigma_c = sigma; P->inv_sigma_c = P->inv_sigma; P->q_c = q; P->g_c = P->g;
+      P->rc_c = P->rc; P->delta_c = delta; P->exact_c = P->exact_t1;
+    }
     P->gfast = (kt == KS_GAUSSIAN && P->exact_t1 && !P->any_flag) ? 1 : 0;
     P->ff_ok = (s_mx[0] <= 0x1p50) ? 1 : 0;
   }
@@ -387,11 +418,14 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntask) return;
   const KParams kp = kps[t];
-  const double delta = P->delta;
+  const bool centred = kt_uses_norms(kp.type);
+  const double delta = centred ? P->delta_c : P->delta;
   TaskParam T;
   T.kp = kp;
   T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.lap = LapParam{0, 0, 0.f, 0.f, 0.f, {0, 0, 0}};
-  T.centred = kt_uses_norms(kp.type) ? 1 : 0;
+  T.centred = centred ? 1 : 0;
+  T.rc = centred ? P->rc_c : P->rc;
+  T.exact = centred ? P->exact_c : P->exact_t1;
   if (kp.type == KS_GAUSSIAN) {
     const double s2 = kp.scal * 1.4426950408889634;
     T.s2 = (float)s2;
@@ -450,7 +484,10 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   }
   const int pidx = valid ? pool_index(map, pt, npool, err) : 0;
   const double *x = X + (size_t)pidx * k;
-  const double sc = P->alpha * P->inv_sigma * 128.0;        // coordinate -> slice units
+  // the list's distance tasks take the centred scale
+  const bool cs = tiles != nullptr && centred;
+  const double sigma = cs ? P->sigma_c : P->sigma;
+  const double sc = P->alpha * (cs ? P->inv_sigma_c : P->inv_sigma) * 128.0;   // coordinate -> slice units
   uint8_t *base = img + (size_t)tile * tile_bytes(BM, kpad);
   const size_t bb = blk_bytes(BM, kpad);
   // The norm of the represented point restricted to the products the tensor
@@ -493,9 +530,9 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   // The norm in units of the accumulators: nu = |x''|^2 / g with
   // g = 2 sigma^2 2^-14, so that d2 = g (nu_i + nu_j - H - L).  nu is split on
   // the grid q / g (a power of two): its high parts and H add exactly.
-  const double g = P->g;
-  const double nu = nrm * (P->sigma * P->sigma) / g;
-  const double qg = P->q / g;
+  const double g = cs ? P->g_c : P->g;
+  const double nu = nrm * (sigma * sigma) / g;
+  const double qg = (cs ? P->q_c : P->q) / g;
   const double nh = rint(nu / qg) * qg;
   const double nl = nu - nh;
   PtMeta mt;
@@ -1449,23 +1486,25 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         const uint32_t tH = tmem + ((uint32_t)(qd * 32) << 16) + buf * 256;
         const bool dump = a.dump && blockIdx.x == 0 && tc == 0;
         if constexpr (KT == KS_LIST) {
+          const float lrc = T.rc;              // the task's scale (centred or not)
+          const bool lexact = T.exact != 0;
           switch (T.kp.type) {
             case KS_GAUSSIAN:
-              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
             case KS_POLYNOMIAL:
-              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
             case KS_TANH:
-              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
             case KS_QUARTIC:
-              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
             case KS_MULTIQUADRATIC:
-              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
             default:
-              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, rc, exact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
           }
         } else {
           tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, ltab, racc, bsk);
