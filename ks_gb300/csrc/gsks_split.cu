@@ -121,11 +121,11 @@ struct Params {          // per call, computed on the device
   int ff_ok;             // coordinates within 2^50: float-pair rechecks stay in range
   LapParam lap;          // Laplace exponent constants
   double delta;          // absolute error bound of the assembled d2 (scaled units)
-  // The list form's distance tasks (coordinates taken relative to the centre)
-  // use their own, finer scale; single calls repeat the one above.
-  double sigma_c, inv_sigma_c, q_c, g_c, delta_c;
-  float rc_c;
-  int exact_c;
+  // List form: the bounding box's largest half-extent and sum of squared
+  // half-extents, centred (distance tasks) and uncentred (inner-product
+  // tasks); each task's scale follows from them (task_params_kernel).
+  double mx_c, sq_c, mx_u, sq_u;
+  int k;
 };
 
 // Kernel selector of the batched (list) form: the epilogue dispatches on each
@@ -145,6 +145,11 @@ struct __align__(16) TaskParam {
   int centred;           // distance kernels: coordinates taken relative to the centre
   float rc;              // -g of the task's scale (d2 = g (nu_i + nu_j - H - L))
   int exact;             // nu_i + nu_j - H is exact in FP32 at that scale
+  // the task's tile images: coordinate -> slice units, sigma^2, g and the norm
+  // grid q (list form; Gaussian tasks are scaled by their bandwidth)
+  double sc, sig2, g, q;
+  int gfast;             // Gaussian without flags: low norm parts folded (as Params::gfast)
+  int pad[3];
 };
 static_assert(sizeof(TaskParam) % 16 == 0, "TaskParam is copied by the bulk-copy engine");
 
@@ -343,19 +348,10 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0 && kt == KS_LIST) {
-    // the centred scale of the list's distance tasks (alpha = 1)
-    const double maxabs = s_mxc[0];
-    double sigma = maxabs > 0.0 ? exp2(ceil(log2(maxabs))) : 1.0;
-    if (sigma < maxabs) sigma *= 2.0;
-    const double nbound = s_sqc[0];
-    const double q = exp2(ceil(log2(2.0 * nbound + 1e-300)) - 23.0);
-    P->sigma_c = sigma; P->inv_sigma_c = 1.0 / sigma; P->q_c = q;
-    P->g_c = 2.0 * sigma * sigma * 0x1p-14;
-    P->rc_c = (float)(-P->g_c);
-    P->delta_c = 2.0 * (sigma * sigma * (double)k * 0x1p-31) +
-                 2.0 * sigma * sqrt((double)k) * sqrt(nbound) * 0x1p-30 + 2.0 * q * 0x1p-23;
-    P->exact_c = (q <= P->g_c) ? 1 : 0;
+  if (threadIdx.x == 0) {
+    P->k = k;
+    P->mx_c = s_mxc[0]; P->sq_c = s_sqc[0];
+    P->mx_u = s_mx[0]; P->sq_u = s_sq[0];
   }
   if (threadIdx.x == 0) {
     const double log2e = 1.4426950408889634;
@@ -400,18 +396,17 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     // 2 sigma^2 2^-14; when the latter is a multiple of q their sum is exact
     // (it stays below 2^24 q), and only the small L term needs Fast2Sum.
     P->exact_t1 = (q <= 2.0 * sigma * sigma * 0x1p-14) ? 1 : 0;
-    if (kt != KS_LIST) {
-      P->sigma_c = sigma; P->inv_sigma_c = P->inv_sigma; P->q_c = q; P->g_c = P->g;
-      P->rc_c = P->rc; P->delta_c = delta; P->exact_c = P->exact_t1;
-    }
     P->gfast = (kt == KS_GAUSSIAN && P->exact_t1 && !P->any_flag) ? 1 : 0;
     P->ff_ok = (s_mx[0] <= 0x1p50) ? 1 : 0;
   }
 
 }
 
-// Per-task epilogue parameters of the list form (coordinates unscaled, alpha = 1):
-// the flag thresholds of params_kernel with each task's own kernel.
+// Per-task parameters of the list form: the scale of the task's tile images
+// and the flag thresholds, by the rules of params_kernel with the task's own
+// kernel.  Distance tasks take the centred box, inner-product tasks the
+// uncentred one; Gaussian tasks fold their bandwidth into the coordinates
+// (scaled units, as a single call), the others keep them unscaled.
 __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, const Params *__restrict__ P,
                                    float tau, TaskParam *__restrict__ out)
 {
@@ -419,19 +414,36 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   if (t >= ntask) return;
   const KParams kp = kps[t];
   const bool centred = kt_uses_norms(kp.type);
-  const double delta = centred ? P->delta_c : P->delta;
+  const double s2 = kp.scal * 1.4426950408889634;
+  const double alpha = kp.type == KS_GAUSSIAN ? sqrt(fmax(-s2, 0.0)) : 1.0;
+  const double maxabs = alpha * (centred ? P->mx_c : P->mx_u);
+  double sigma = maxabs > 0.0 ? exp2(ceil(log2(maxabs))) : 1.0;
+  if (sigma < maxabs) sigma *= 2.0;
+  const double nbound = alpha * alpha * (centred ? P->sq_c : P->sq_u);
+  const double q = exp2(ceil(log2(2.0 * nbound + 1e-300)) - 23.0);
+  const double g = 2.0 * sigma * sigma * 0x1p-14;
+  const int k = P->k;
+  const double delta = 2.0 * (sigma * sigma * (double)k * 0x1p-31) +
+                       2.0 * sigma * sqrt((double)k) * sqrt(nbound) * 0x1p-30 + 2.0 * q * 0x1p-23;
   TaskParam T;
   T.kp = kp;
   T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.lap = LapParam{0, 0, 0.f, 0.f, 0.f, {0, 0, 0}};
   T.centred = centred ? 1 : 0;
-  T.rc = centred ? P->rc_c : P->rc;
-  T.exact = centred ? P->exact_c : P->exact_t1;
+  T.sc = alpha / sigma * 128.0;
+  T.sig2 = sigma * sigma;
+  T.g = g;
+  T.q = q;
+  T.rc = (float)(-g);
+  T.exact = (q <= g) ? 1 : 0;
+  T.gfast = 0;
+  T.pad[0] = T.pad[1] = T.pad[2] = 0;
   if (kp.type == KS_GAUSSIAN) {
-    const double s2 = kp.scal * 1.4426950408889634;
-    T.s2 = (float)s2;
+    T.s2 = (float)s2;                      // the rechecks work from the pool coordinates
     T.s2l = (float)(s2 - (double)T.s2);
-    // relative error of 2^(s2 d2) is ln2 |s2| delta; beyond d2 = 126 / |s2| it underflows
-    if (0.6931471805599453 * fabs(s2) * delta > tau) T.t_flag = (float)(126.0 / fabs(s2));
+    // scaled units: the relative error of 2^-d2 is ln2 delta; pairs with
+    // d2 >= 126 underflow anyway
+    if (0.6931471805599453 * delta > tau) T.t_flag = 126.0f;
+    T.gfast = (T.exact && T.t_flag < 0.0f) ? 1 : 0;
   } else if (kp.type == KS_GAUSSIAN_VAR_BANDWIDTH) {
     T.t_flag = (float)(tau / (0.6931471805599453 * delta));   // cap on f, as params_kernel
   } else if (kp.type == KS_LAPLACE) {
@@ -484,10 +496,11 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   }
   const int pidx = valid ? pool_index(map, pt, npool, err) : 0;
   const double *x = X + (size_t)pidx * k;
-  // the list's distance tasks take the centred scale
-  const bool cs = tiles != nullptr && centred;
-  const double sigma = cs ? P->sigma_c : P->sigma;
-  const double sc = P->alpha * (cs ? P->inv_sigma_c : P->inv_sigma) * 128.0;   // coordinate -> slice units
+  // coordinate -> slice units: the call's scale, or the list task's
+  const TaskParam *TT = tiles ? &tp[tile_task[tile]] : nullptr;
+  const double sc = TT ? TT->sc : P->alpha * P->inv_sigma * 128.0;
+  const double sig2 = TT ? TT->sig2 : P->sigma * P->sigma;
+  const bool gfast = TT ? TT->gfast != 0 : P->gfast != 0;
   uint8_t *base = img + (size_t)tile * tile_bytes(BM, kpad);
   const size_t bb = blk_bytes(BM, kpad);
   // The norm of the represented point restricted to the products the tensor
@@ -530,9 +543,9 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   // The norm in units of the accumulators: nu = |x''|^2 / g with
   // g = 2 sigma^2 2^-14, so that d2 = g (nu_i + nu_j - H - L).  nu is split on
   // the grid q / g (a power of two): its high parts and H add exactly.
-  const double g = cs ? P->g_c : P->g;
-  const double nu = nrm * (sigma * sigma) / g;
-  const double qg = (cs ? P->q_c : P->q) / g;
+  const double g = TT ? TT->g : P->g;
+  const double nu = nrm * sig2 / g;
+  const double qg = (TT ? TT->q : P->q) / g;
   const double nh = rint(nu / qg) * qg;
   const double nl = nu - nh;
   PtMeta mt;
@@ -541,7 +554,7 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   mt.w = 0.0f;
   mt.h = 0.0f;
   if (side == 1 && valid) mt.w = (float)w[wmap ? wmap[pt] : pt];
-  if (P->gfast) {
+  if (gfast) {
     // Gaussian: 2^-(g nl) is a per-point factor; fold it into w for sources
     // and into a row factor for targets (applied to the row sum)
     const double f = exp2(-g * nl);
@@ -1122,8 +1135,10 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
   return flags;
 }
 
-// NC columns of one row, inner-product kernels (polynomial, tanh).
-template <int KT, int NC>
+// NC columns of one row, inner-product kernels (polynomial, tanh).  PW in
+// 1..4: a polynomial of that integer power, multiplied out; its values are
+// finite on padding columns (x.y = 0 there), whose weight 0 then needs no mask.
+template <int KT, int NC, int PW = 0>
 __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                              const SrcMeta *__restrict__ bm, int c0, int valid, float rc,
                                              const KParams &kp, float (&acc)[4])
@@ -1143,6 +1158,15 @@ __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint
       const uint64_t H = pk2(__uint_as_float(h[j]), __uint_as_float(h[j + 1]));
       const uint64_t L = pk2(__uint_as_float(l[j]), __uint_as_float(l[j + 1]));
       const uint64_t CC = mul2(fma2(L, RC, mul2(H, RC)), MH);          // x.y
+      if constexpr (PW > 0) {
+        const uint64_t V = fma2(SC, CC, CN);
+        uint64_t R = V;
+        if constexpr (PW == 2) R = mul2(V, V);
+        if constexpr (PW == 3) R = mul2(mul2(V, V), V);
+        if constexpr (PW == 4) { R = mul2(V, V); R = mul2(R, R); }
+        A[p2] = fma2(R, pk2(f4(ww, 2 * p2), f4(ww, 2 * p2 + 1)), A[p2]);
+        continue;
+      }
       float k0, k1;
       if (ipow) {
         // (scal x.y + cons)^p by binary powering on both columns
@@ -1263,6 +1287,13 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
           nchk = true;
         }
       }
+    } else if constexpr (KT == KS_POLYNOMIAL) {
+      const int pw = T.kp.pmode == POW_INT ? T.kp.pint : 0;
+      if (pw == 2) epi_chunk_ip<KT, NCH, 2>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else if (pw == 3) epi_chunk_ip<KT, NCH, 3>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else if (pw == 4) epi_chunk_ip<KT, NCH, 4>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else if (pw == 1) epi_chunk_ip<KT, NCH, 1>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else epi_chunk_ip<KT, NCH>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
     } else {
       epi_chunk_ip<KT, NCH>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
     }
@@ -1489,8 +1520,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           const float lrc = T.rc;              // the task's scale (centred or not)
           const bool lexact = T.exact != 0;
           switch (T.kp.type) {
-            case KS_GAUSSIAN:
-              tile_epilogue<KS_GAUSS_UNSCALED>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
+            case KS_GAUSSIAN:   // scaled units, as a single call
+              tile_epilogue<KS_GAUSSIAN>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, dump, ltab, racc, bsk); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
               tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
             case KS_POLYNOMIAL:
@@ -1521,7 +1552,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");
       if (grp == 0) {
         for (int q = 0; q < EPI_GROUPS - 1; q++) { racc += xs[q][row]; bsk += xb[q][row]; }
-        if (KT == KS_GAUSSIAN && gfast) {         // the row's low-norm factor
+        const bool rowf = KT == KS_LIST ? (T.kp.type == KS_GAUSSIAN && T.gfast != 0) : (KT == KS_GAUSSIAN && gfast);
+        if (rowf) {                               // the row's low-norm factor
           racc *= (double)am.h;
           bsk *= am.h;
         }
