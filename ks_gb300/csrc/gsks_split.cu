@@ -67,7 +67,7 @@ constexpr int KPAD_MAX = 64;        // padded k of the target-resident kernel
 constexpr int NSTAGE = 3;           // source-tile operand stages
 constexpr int LTAB = 256;           // Laplace log2 table entries
 constexpr size_t SMEM_MAX = 232448; // dynamic shared memory per block (227 KB)
-constexpr int NMETA = 4;            // source-tile metadata ring
+constexpr int NMETA = 3;            // source-tile metadata ring
 constexpr int NBLK = 3;             // slices per operand
 constexpr int EPI_GROUPS = 4;          // column groups of the epilogue
 constexpr int EPI_WARPS = 4 * EPI_GROUPS;
@@ -649,6 +649,7 @@ struct SplitSmem {
   int never;             // stays 0: an abort flag for the drain waits
   double rsum[2][EPI_GROUPS - 1][BM];   // row sums of epilogue groups 1.., by item parity
   float rskip[2][EPI_GROUPS - 1][BM];   // their skipped-group weights (pskip)
+  float rq[EPI_WARPS][32];              // per epilogue warp: recheck values (recheck_warp)
   TaskParam tslot[2];    // list form: the current items' task parameters, by item parity
   int islot[2];          // the current items (-1: no work left), by item parity
 };
@@ -660,6 +661,20 @@ __host__ __device__ inline size_t smem_fixed(const SmemLayout &L)
   return 1024 /* alignment slack */ + L.a_region + L.nstage * L.stage_bytes + NMETA * (size_t)BN * sizeof(PtMeta) +
          sizeof(SplitSmem) + 64;
 }
+
+// The largest non-table layout (resident k = KPAD_MAX, NSTAGE source stages)
+// fits the shared memory of a block.
+static_assert(1024 + ((NBLK * (size_t)BM * KPAD_MAX * 2 + (size_t)BM * sizeof(PtMeta) + 1023) & ~(size_t)1023) +
+                      NSTAGE * ((NBLK * (size_t)BM * KPAD_MAX * 2 + 1023) & ~(size_t)1023) +
+                      NMETA * (size_t)BN * sizeof(PtMeta) + sizeof(SplitSmem) + 64 <= SMEM_MAX,
+              "split_tiles shared memory");
+// The streaming layout (k beyond KPAD_MAX: two stages of both operands' 64-wide
+// chunks) with one copy of the Laplace table (the list form) fits too.
+static_assert(1024 + (((size_t)BM * sizeof(PtMeta) + 1023) & ~(size_t)1023) +
+                      2 * 2 * ((NBLK * (size_t)BM * KCH * 2 + 1023) & ~(size_t)1023) +
+                      NMETA * (size_t)BN * sizeof(PtMeta) + sizeof(SplitSmem) + 64 + ((sizeof(SplitSmem) + 15) & 15) +
+                      (size_t)LTAB * 16 <= SMEM_MAX,
+              "split_tiles shared memory (streaming, table)");
 
 template <int KT>
 __device__ __forceinline__ const TaskParam &pick_task(const TaskParam &slot, const TaskParam &single)
@@ -953,10 +968,10 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
 // the pools' float-pair copies, then exp2_prod) times the column's FP32 weight
 // is formed in FP32 like the main path's.  Needs the copies (ffp).
 template <int KT>
-__device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T, const PtMeta &am,
+__device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T, int ipos, float ah, float ahl,
                                            const SrcMeta *__restrict__ bm, int c)
 {
-  const int ipos = am.pos, jpos = bm->pos[c];
+  const int jpos = bm->pos[c];
   int pa = a.amap ? a.amap[ipos] : ipos;
   int pb = a.bmap ? a.bmap[jpos] : jpos;
   if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
@@ -966,7 +981,7 @@ __device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T
   float ph, pl;
   if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
     // (-0.5 log2e hi) hj from the row's and the column's float pairs
-    const float ah = am.h, ahl = __int_as_float(am.pad[1]), hc = bm->h[c], hl = bm->hlo[c];
+    const float hc = bm->h[c], hl = bm->hlo[c];
     ph = ah * hc;
     pl = fmaf(ah, hc, -ph) + fmaf(ah, hl, ahl * hc);
   } else {
@@ -974,6 +989,59 @@ __device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T
     pl = T.s2l;
   }
   return exp2_prod(th, tl, ph, pl) * bm->w[c];
+}
+
+// The flagged pairs of one warp's 32 rows (lanes) x 32 columns, all lanes
+// working: the flags are numbered lane by lane (fl: this lane's columns, bit
+// j = column 32 grp + j), 32 per round; each lane rechecks one (recheck_f),
+// and each row adds its own values in their order (through the warp's
+// 32-float scratch wq) to add, their magnitudes to fchk.
+template <int KT>
+__device__ __forceinline__ void recheck_warp(const TileArgs &a, const TaskParam &T, const PtMeta &am,
+                                             const SrcMeta *__restrict__ bm, int grp, uint32_t fl,
+                                             float *wq, float &add, float &fchk)
+{
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int cnt = __popc(fl);
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int excl = incl - cnt;
+  const int tot = __shfl_sync(full, incl, 31);
+  for (int base = 0; base < tot; base += 32) {
+    const int e = base + lane;
+    int L = 0;                       // the owner: lanes before it have incl <= e
+#pragma unroll
+    for (int st = 16; st > 0; st >>= 1) {
+      const int v = __shfl_sync(full, incl, L + st - 1);
+      if (v <= e) L += st;
+    }
+    L = min(L, 31);                  // e >= tot: no entry
+    const uint32_t flL = __shfl_sync(full, fl, L);
+    const int exL = __shfl_sync(full, excl, L);
+    const int posL = __shfl_sync(full, am.pos, L);
+    const float hL = __shfl_sync(full, am.h, L);
+    const float hlL = __shfl_sync(full, __int_as_float(am.pad[1]), L);
+    float v = 0.f;
+    if (e < tot) {
+      uint32_t mk = flL;             // its (e - exL)-th flagged column
+      for (int i = e - exL; i > 0 && mk; i--) mk &= mk - 1;
+      if (mk) v = recheck_f<KT>(a, T, posL, hL, hlL, bm, grp * 32 + __ffs(mk) - 1);
+    }
+    wq[lane] = v;
+    __syncwarp();
+    const int q1 = min(incl, base + 32) - base;
+    for (int q = max(excl, base) - base; q < q1; q++) {
+      const float x = wq[q];
+      add += x;
+      fchk += fabsf(x);
+    }
+    __syncwarp();
+  }
 }
 
 // Squared distance t + lo (double-float, scaled units) of one pair from its
@@ -1234,8 +1302,12 @@ template <int KT>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
                                               const SrcMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
                                               bool gfast, bool dump, const LTab &ltab, double &racc,
-                                              float &bsk)
+                                              float &bsk, float *wq)
 {
+  // Gaussian kinds with the pools' float-pair copies: flagged pairs are
+  // collected over the 32 columns (fl32) and rechecked by the whole warp
+  constexpr bool GK = KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH;
+  uint32_t fl32 = 0;
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   double rchk = 0.0;
   float fchk = 0.f;                 // |rechecked values|, for the underflow test
@@ -1267,20 +1339,18 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
         if (fl) flags = epi_chunk<KT, false, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
         else epi_chunk<KT, false, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
       }
-      // rechecks of the flagged pairs of these columns
+      if constexpr (GK) {
+        if (ffp) {
+          fl32 |= flags << (part * NCH);
+          flags = 0;
+        }
+      }
+      // rechecks of the flagged pairs of these columns (one lane each)
       while (flags) {
         const int j = __ffs(flags) - 1;
         flags &= flags - 1;
         const int c = c0 + j;
         if (c < ncols && am.pos >= 0) {
-          if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
-            if (ffp) {
-              const float v = recheck_f<KT>(a, T, am, bm, c);
-              acc[0] += v;
-              fchk += fabsf(v);
-              continue;
-            }
-          }
           const double v = recheck<KT>(a, T, ltab, am.pos, bm->pos[c]);
           rchk += v;
           fchk += fabsf((float)v);
@@ -1296,6 +1366,18 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
       else epi_chunk_ip<KT, NCH>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
     } else {
       epi_chunk_ip<KT, NCH>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+    }
+  }
+  if constexpr (GK) {
+    if (ffp) {
+      const int nv = ncols - grp * 32;   // valid columns of the group
+      if (am.pos < 0 || nv <= 0) fl32 = 0;
+      else if (nv < 32) fl32 &= (1u << nv) - 1u;
+      if (__any_sync(0xffffffffu, fl32 != 0)) {
+        float add = 0.f;
+        recheck_warp<KT>(a, T, am, bm, grp, fl32, wq, add, fchk);
+        acc[0] += add;
+      }
     }
   }
   const float fs = (acc[0] + acc[1]) + (acc[2] + acc[3]);
@@ -1481,6 +1563,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     // sub-partition, in two 16-column TMEM loads.
     const int ew = warp - 2;
     const int grp = ew >> 2;
+    float *wq = S->rq[ew];
     const LTab ltab{tab_base + (L.tab_sh > 0 ? (lane & ((1 << L.tab_sh) - 1)) : 0), L.tab_sh > 0 ? L.tab_sh : 0};
     const int qd = warp & 3;
     const int row = qd * 32 + lane;
@@ -1521,24 +1604,24 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           const bool lexact = T.exact != 0;
           switch (T.kp.type) {
             case KS_GAUSSIAN:   // scaled units, as a single call
-              tile_epilogue<KS_GAUSSIAN>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_GAUSSIAN>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, dump, ltab, racc, bsk, wq); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             case KS_POLYNOMIAL:
-              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             case KS_TANH:
-              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             case KS_QUARTIC:
-              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             case KS_MULTIQUADRATIC:
-              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             default:
-              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk); break;
+              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
           }
         } else {
-          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, ltab, racc, bsk);
+          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, ltab, racc, bsk, wq);
         }
         tc_fence_before();
         __syncwarp();
