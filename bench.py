@@ -353,7 +353,7 @@ def run_ours(args, ws, rank, local):
         t = dk["ms"] * 1e-3
         roof = {"bound": "tensor", "kernel": f"split_tiles<{dom}>", "achieved": dk["alg_tflops"],
                 "peak": round(peaks.get("bf16_tflops", 1900.0), 1), "unit": "TFLOP/s",
-                "frac": dk["frac_alg_tensor"], "traffic": read_traffic(f"split_tiles_{dom}_c2"),
+                "frac": dk["frac_alg_tensor"], "traffic": read_traffic(f"split_tiles_{dom}_general_stride"),
                 "flops": "algorithmic 2mnk per launch; the split form executes 6 f16 products per slice set "
                          "(executed_tflops)",
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst; f16 runs at the bf16 rate)"
@@ -361,7 +361,7 @@ def run_ours(args, ws, rank, local):
     else:
         roof = {"bound": "fp64", "kernel": f"fp64_tiles<{dom}>", "achieved": dk["achieved_tflops"],
                 "peak": round(2 * rates["dfma"] / 1e12, 4), "unit": "TFLOP/s", "frac": dk["frac"],
-                "traffic": read_traffic(f"fp64_tiles_{dom}_c2"),
+                "traffic": read_traffic(f"fp64_tiles_{dom}_general_stride"),
                 "peak_source": "measured live: gsks_probe_peak FP64 FMA rate x 2"}
     roof["per_form"] = {f: results[f]["per_kernel"] for f in forms}
     roof["pipe_rates_measured"] = {k: float("%.4g" % v) for k, v in rates.items()}
