@@ -105,7 +105,8 @@ struct LapParam {
   int P, ls13;
   float lsf, mh;         // mh = -P/2
   float tover;           // d2 below tover: K may exceed the FP32 range
-  int pad[3];
+  int c0, p4096;         // ls13 + 127 P 4096 and P 4096: E = c0 - p4096 (bits >> 23) - P z
+  int pad;
 };
 
 struct Params {          // per call, computed on the device
@@ -309,7 +310,9 @@ __device__ LapParam lap_param(double scal, double powe)
   L.mh = -0.5f * (float)L.P;
   const double mm = -powe;
   L.tover = (float)(pow(scal, 1.0 / mm) * exp2(-120.0 / mm) * 1.001);   // K = 2^120 at d2 = c0 2^(-120/m)
-  L.pad[0] = L.pad[1] = L.pad[2] = 0;
+  L.c0 = L.ls13 + 127 * 4096 * L.P;
+  L.p4096 = 4096 * L.P;
+  L.pad = 0;
   return L;
 }
 
@@ -427,7 +430,7 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
                        2.0 * sigma * sqrt((double)k) * sqrt(nbound) * 0x1p-30 + 2.0 * q * 0x1p-23;
   TaskParam T;
   T.kp = kp;
-  T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.lap = LapParam{0, 0, 0.f, 0.f, 0.f, {0, 0, 0}};
+  T.t_flag = -1.0f; T.rho = 0.0f; T.s2 = T.s2l = 0.0f; T.lap = LapParam{0, 0, 0.f, 0.f, 0.f, 0, 0, 0};
   T.centred = centred ? 1 : 0;
   T.sc = alpha / sigma * 128.0;
   T.sig2 = sigma * sigma;
@@ -738,7 +741,8 @@ __device__ __forceinline__ float laplace_val(float t, float lo, const LTab &tab,
   return n >= -126 ? y * __int_as_float((n + 127) << 23) : 0.0f;
 }
 
-// laplace_val of two columns, the floating-point part in packed FP32 pairs.
+// laplace_val of two columns, the floating-point part in packed FP32 pairs (the
+// series one term shorter: its error stays far below the per-pair budget).
 __device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const LTab &tab, const LapParam &L)
 {
   const float t0 = lo2(T), t1 = hi2(T);
@@ -747,18 +751,25 @@ __device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const 
   const uint64_t F = pk2(__uint_as_float((u0 & 0x007fffffu) | 0x3f800000u),
                          __uint_as_float((u1 & 0x007fffffu) | 0x3f800000u));
   const uint64_t R = fma2(F, pk2(b0.x, b1.x), pk2(-1.0f, -1.0f));
-  uint64_t Q = fma2(R, pk2(-0.36067376f, -0.36067376f), pk2(0.48089835f, 0.48089835f));
-  Q = fma2(R, Q, pk2(-0.72134752f, -0.72134752f));
+  // log2(1 + r) to r^3: the omitted -log2(e) r^4 / 4 is below 2^-36.7 (|r| < 2^-8.8),
+  // 2^-27.7 relative on K even at P = 1022
+  uint64_t Q = fma2(R, pk2(0.48089835f, 0.48089835f), pk2(-0.72134752f, -0.72134752f));
   Q = mul2(R, fma2(R, Q, pk2(1.44269504f, 1.44269504f)));
   const uint64_t RT = pk2(rcp_approx(t0), rcp_approx(t1));
-  const uint64_t LLO = add2(add2(pk2(b0.y, b1.y), Q), mul2(mul2(LO, RT), pk2(1.44269504f, 1.44269504f)));
-  const int E0 = L.ls13 - L.P * (((int)(u0 >> 23) - 127) * 4096 + __float_as_int(b0.z));
-  const int E1 = L.ls13 - L.P * (((int)(u1 >> 23) - 127) * 4096 + __float_as_int(b1.z));
-  const uint64_t ARG = fma2(pk2((float)(E0 & 8191), (float)(E1 & 8191)), pk2(0x1p-13f, 0x1p-13f),
-                            fma2(pk2(L.mh, L.mh), LLO, pk2(L.lsf, L.lsf)));
+  const uint64_t LLO = fma2(mul2(LO, RT), pk2(1.44269504f, 1.44269504f), add2(pk2(b0.y, b1.y), Q));
+  // the exponent in 2^-13 units, ls13 - P (4096 (e - 127) + z), with the
+  // constant terms folded into c0 and p4096
+  const int E0 = L.c0 - L.p4096 * (int)(u0 >> 23) - L.P * __float_as_int(b0.z);
+  const int E1 = L.c0 - L.p4096 * (int)(u1 >> 23) - L.P * __float_as_int(b1.z);
+  // its fraction (E mod 8192) 2^-13 exactly: the float 2^23 + (E & 8191) times
+  // 2^-13 is 1024 + fraction, and the FMA with -1024 rounds nothing
+  const uint64_t FR = fma2(pk2(__uint_as_float(0x4B000000u | (uint32_t)(E0 & 8191)),
+                               __uint_as_float(0x4B000000u | (uint32_t)(E1 & 8191))),
+                           pk2(0x1p-13f, 0x1p-13f), pk2(-1024.0f, -1024.0f));
+  const uint64_t ARG = add2(FR, fma2(pk2(L.mh, L.mh), LLO, pk2(L.lsf, L.lsf)));
+  // 2^n, zero below 2^-126
   const int n0 = E0 >> 13, n1 = E1 >> 13;
-  const float s0 = n0 >= -126 ? __int_as_float((n0 + 127) << 23) : 0.0f;
-  const float s1 = n1 >= -126 ? __int_as_float((n1 + 127) << 23) : 0.0f;
+  const float s0 = __int_as_float(max(n0 + 127, 0) << 23), s1 = __int_as_float(max(n1 + 127, 0) << 23);
   return mul2(pk2(ex2_approx(lo2(ARG)), ex2_approx(hi2(ARG))), pk2(s0, s1));
 }
 
@@ -1193,7 +1204,7 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
           const float f = -am.h * f4(hh, q);      // 0.5 log2(e) h_i h_j
           if (f > t_flag && t * f < 126.f) { flags |= 1u << j; kv = 0.f; }
         } else {
-          if (t < t_flag || t < rho * s) { flags |= 1u << j; kv = 0.f; }
+          if (t < fmaxf(t_flag, rho * s)) { flags |= 1u << j; kv = 0.f; }
         }
       }
       // padding columns carry w = 0 and finite distances
