@@ -256,9 +256,18 @@ int list_plan_build(ListPlan &L, Ctx *c, ks_t *kernel, ks_t *kernels, int ntask,
       }
     pbase += (long long)nsc * m;
   }
-  std::stable_sort(items.begin(), items.end(), [](const ListItem &x, const ListItem &y) {
-    return (long long)x.rows * x.cols > (long long)y.rows * y.cols;
-  });
+  {
+    // largest rows x cols first, ties in build order: a counting sort (the
+    // products are bounded by the tile height times the source chunk)
+    int cmax = 0;
+    for (const ListItem &it : items) cmax = std::max(cmax, it.rows * it.cols);
+    std::vector<size_t> start((size_t)cmax + 2, 0);
+    for (const ListItem &it : items) start[(size_t)(cmax - it.rows * it.cols) + 1]++;
+    for (int b = 0; b <= cmax; b++) start[b + 1] += start[b];
+    std::vector<ListItem> sorted(items.size());
+    for (const ListItem &it : items) sorted[start[cmax - it.rows * it.cols]++] = it;
+    items.swap(sorted);
+  }
   L.pbase = pbase;
   L.nitems = (int)items.size();
   bool ok = (L.split || upload(L.items, items.data(), items.size(), s)) &&

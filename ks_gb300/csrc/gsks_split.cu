@@ -1996,28 +1996,46 @@ int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, con
   if (kpad > 1024) return GSKS_ERR_TOO_LARGE;
   const int chunk_tiles = chunk / BN;
 
-  // tiles and items on the host
-  std::vector<int2> ta, tb;
-  std::vector<int> ta_task, tb_task, tb_cols;
-  std::vector<SplitItem> items;
-  std::vector<double> cost;
+  // tiles and items on the host: counts per task, offsets, then every task's
+  // entries filled in parallel (the same order as a serial pass: task, then
+  // source chunk, then target tile)
+  std::vector<int> ota(ntask + 1, 0), otb(ntask + 1, 0);
+  std::vector<long long> oit(ntask + 1, 0);
   long long na = 0, nb = 0;
   for (int t = 0; t < ntask; t++) {
     const int m = hoff_a[t + 1] - hoff_a[t], n = hoff_b[t + 1] - hoff_b[t];
+    const bool live = m > 0 && n > 0;
+    const int ca = live ? (m + BM - 1) / BM : 0, cb = live ? (n + BN - 1) / BN : 0;
+    if (live) { na += m; nb += n; }
+    ota[t + 1] = ota[t] + ca;
+    otb[t + 1] = otb[t] + cb;
+    oit[t + 1] = oit[t] + (long long)ca * ((cb + chunk_tiles - 1) / chunk_tiles);
+  }
+  if (na > INT32_MAX || nb > INT32_MAX || oit[ntask] > INT32_MAX) return GSKS_ERR_TOO_LARGE;
+  std::vector<int2> ta(ota[ntask]), tb(otb[ntask]);
+  std::vector<int> ta_task(ota[ntask]), tb_task(otb[ntask]), tb_cols(otb[ntask]);
+  std::vector<SplitItem> items(oit[ntask]);
+  std::vector<int> cost(oit[ntask]);     // relative epilogue cost: source tiles, x3 for Laplace
+#pragma omp parallel for schedule(dynamic, 64) if (ntask > 512)
+  for (int t = 0; t < ntask; t++) {
+    const int m = hoff_a[t + 1] - hoff_a[t], n = hoff_b[t + 1] - hoff_b[t];
     if (m <= 0 || n <= 0) continue;
-    na += m; nb += n;
-    const int a_base = (int)ta.size(), b_base = (int)tb.size();
-    for (int i0 = 0; i0 < m; i0 += BM) { ta.push_back(make_int2(hoff_a[t] + i0, std::min(BM, m - i0))); ta_task.push_back(t); }
-    for (int j0 = 0; j0 < n; j0 += BN) {
-      tb.push_back(make_int2(hoff_b[t] + j0, std::min(BN, n - j0)));
-      tb_task.push_back(t);
-      tb_cols.push_back(std::min(BN, n - j0));
+    const int a_base = ota[t], b_base = otb[t];
+    for (int i0 = 0; i0 < m; i0 += BM) {
+      ta[a_base + i0 / BM] = make_int2(hoff_a[t] + i0, std::min(BM, m - i0));
+      ta_task[a_base + i0 / BM] = t;
     }
-    const int ntn = (int)tb.size() - b_base;
-    // relative epilogue cost per tile: the Laplace evaluation dominates
-    const double wkt = kps[t].type == KS_LAPLACE ? 3.0 : 1.0;
+    for (int j0 = 0; j0 < n; j0 += BN) {
+      tb[b_base + j0 / BN] = make_int2(hoff_b[t] + j0, std::min(BN, n - j0));
+      tb_task[b_base + j0 / BN] = t;
+      tb_cols[b_base + j0 / BN] = std::min(BN, n - j0);
+    }
+    const int ntn = otb[t + 1] - b_base;
+    // the Laplace evaluation dominates the epilogue
+    const int wkt = kps[t].type == KS_LAPLACE ? 3 : 1;
+    long long q = oit[t];
     for (int sc = 0; sc * chunk_tiles < ntn; sc++)
-      for (int i0 = 0; i0 < m; i0 += BM) {
+      for (int i0 = 0; i0 < m; i0 += BM, q++) {
         SplitItem it{};
         it.a_tile = a_base + i0 / BM;
         it.b0 = b_base + sc * chunk_tiles;
@@ -2025,19 +2043,22 @@ int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, con
         it.task = t;
         it.out = pbase[t] + (long long)sc * m + i0;
         it.rows = std::min(BM, m - i0);
-        items.push_back(it);
-        cost.push_back(wkt * (it.b1 - it.b0));
+        items[q] = it;
+        cost[q] = wkt * (it.b1 - it.b0);
       }
   }
   {
-    std::vector<int> ord(items.size());
-    for (size_t i = 0; i < ord.size(); i++) ord[i] = (int)i;
-    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+    // largest cost first, ties in build order: a counting sort over the few
+    // distinct costs (bucket cmax - cost)
+    int cmax = 0;
+    for (const int c : cost) cmax = std::max(cmax, c);
+    std::vector<size_t> start((size_t)cmax + 2, 0);
+    for (const int c : cost) start[(size_t)(cmax - c) + 1]++;
+    for (int b = 0; b <= cmax; b++) start[b + 1] += start[b];
     std::vector<SplitItem> sorted(items.size());
-    for (size_t i = 0; i < ord.size(); i++) sorted[i] = items[ord[i]];
+    for (size_t i = 0; i < items.size(); i++) sorted[start[cmax - cost[i]]++] = items[i];
     items.swap(sorted);
   }
-  if (na > INT32_MAX || nb > INT32_MAX) return GSKS_ERR_TOO_LARGE;
   std::vector<SplitTaskGeo> tg(ntask);
   long long ptotal = 0;
   for (int t = 0; t < ntask; t++) {
