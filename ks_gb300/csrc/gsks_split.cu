@@ -130,9 +130,8 @@ struct Params {          // per call, computed on the device
 };
 
 // Kernel selector of the batched (list) form: the epilogue dispatches on each
-// task's type; the Gaussian then takes its scale per task (coordinates unscaled).
+// task's type, with the task's own tile scale.
 constexpr int KS_LIST = 99;
-constexpr int KS_GAUSS_UNSCALED = 100;
 
 // Epilogue parameters of one task (a single call uses one, built from Params).
 // The list form copies each item's entry into shared memory with the target
@@ -140,7 +139,7 @@ constexpr int KS_GAUSS_UNSCALED = 100;
 struct __align__(16) TaskParam {
   KParams kp;
   float t_flag, rho;     // flag pairs with t < t_flag or t < rho * (n_i + n_j)
-  float s2, s2l;         // Gaussian of the list form: scal * log2(e) = s2 + s2l
+  float s2, s2l;         // Gaussian rechecks from pool coordinates: scal * log2(e) = s2 + s2l
   LapParam lap;          // Laplace
   int any_flag;
   int centred;           // distance kernels: coordinates taken relative to the centre
@@ -826,12 +825,6 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
   if constexpr (KT == KS_GAUSSIAN) {
     const float e = ex2_approx(-t);
     return fmaf(e, -0.69314718f * lo, e);
-  } else if constexpr (KT == KS_GAUSS_UNSCALED) {
-    // arg2 = s2 (t + lo), s2 = scal log2(e) passed in hrow
-    const float a = t * hrow;
-    const float ae = fmaf(t, hrow, -a) + lo * hrow;
-    const float e = ex2_approx(a);
-    return fmaf(e, 0.69314718f * ae, e);
   } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
     // arg2 = (t + lo) * hrow * hcol, hrow = -0.5 log2e hi
     const float f = hrow * hcol;
@@ -883,7 +876,7 @@ __device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb
   for (int p = 0; p < a.k; p++) { const double d = x[p] - y[p]; d2 = fma(d, d, d2); }
   const double wv = a.w[a.wmap ? a.wmap[jpos] : jpos];
   double kv;
-  if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED) kv = exp(d2 * kp.scal);
+  if constexpr (KT == KS_GAUSSIAN) kv = exp(d2 * kp.scal);
   else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) kv = exp(((d2 * -0.5) * kp.hi[pa]) * kp.hj[pb]);
   else if constexpr (KT == KS_LAPLACE) {
     if (d2 < 1e-15) d2 = 1.79e308;
@@ -935,7 +928,7 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
   int pb = a.bmap ? a.bmap[jpos] : jpos;
   if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
   if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
-  if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH ||
+  if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSSIAN_VAR_BANDWIDTH ||
                 KT == KS_LAPLACE) {
     if (a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag)) {   // the copies exist
       // (a single call builds them only when it may flag pairs)
@@ -953,7 +946,7 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
       ff_dist2(x, y, a.k, th, tl);
       const double wv = a.w[a.wmap ? a.wmap[jpos] : jpos];
       bool deep = false;
-      if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED) {
+      if constexpr (KT == KS_GAUSSIAN) {
         const double v = exp2_prod_wide(th, tl, T.s2, T.s2l, deep) * wv;
         if (!deep) return v;
       } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
@@ -1169,10 +1162,6 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
     if constexpr (KT == KS_LAPLACE) {
       KV2[0] = laplace_val2(T2[0], LO2[0], ltab, T.lap);
       KV2[1] = laplace_val2(T2[1], LO2[1], ltab, T.lap);
-    } else if constexpr (KT == KS_GAUSS_UNSCALED) {
-      const uint64_t S2h = pk2(T.s2, T.s2), S2l = pk2(T.s2l, T.s2l);
-      KV2[0] = exp2_prod2(T2[0], LO2[0], S2h, S2l);
-      KV2[1] = exp2_prod2(T2[1], LO2[1], S2h, S2l);
     } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
       // factor h_i h_j (negative) as a float pair, two columns at a time
       const uint64_t AH = pk2(am.h, am.h), AHL = pk2(__int_as_float(am.pad[1]), __int_as_float(am.pad[1]));
@@ -1191,13 +1180,12 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
       const float lo = (q & 1) ? hi2(LO2[q >> 1]) : lo2(LO2[q >> 1]);
       const float s = (q & 1) ? hi2(S2[q >> 1]) : lo2(S2[q >> 1]);
       float kv;
-      if constexpr (KT == KS_LAPLACE || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH)
+      if constexpr (KT == KS_LAPLACE || KT == KS_GAUSSIAN_VAR_BANDWIDTH)
         kv = (q & 1) ? hi2(KV2[q >> 1]) : lo2(KV2[q >> 1]);
       else kv = kval32<KT>(t, lo, 0.f, am.h, 0.f, kp);
       // smallest exponent (log2 units) of the exponential kernels' values: the
       // row rescue is needed only if some value is not 0 in FP64 either
       if constexpr (KT == KS_GAUSSIAN) amin = fminf(amin, t);
-      else if constexpr (KT == KS_GAUSS_UNSCALED) amin = fminf(amin, -T.s2 * t);
       else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) amin = fminf(amin, -am.h * f4(hh, q) * t);
       if constexpr (FLAGS) {
         if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
@@ -1300,7 +1288,7 @@ __device__ void dump_chunk(float *dump, int row, int c0, const uint32_t (&h)[NC]
 // them (the row rescue of tile_epilogue).
 __host__ __device__ constexpr bool kt_rescue(int kt)
 {
-  return kt == KS_GAUSSIAN || kt == KS_GAUSS_UNSCALED || kt == KS_GAUSSIAN_VAR_BANDWIDTH || kt == KS_LAPLACE;
+  return kt == KS_GAUSSIAN || kt == KS_GAUSSIAN_VAR_BANDWIDTH || kt == KS_LAPLACE;
 }
 
 // One warp's share of one tile (32 columns of its 32 rows): TMEM loads, kernel
@@ -1317,7 +1305,7 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
 {
   // Gaussian kinds with the pools' float-pair copies: flagged pairs are
   // collected over the 32 columns (fl32) and rechecked by the whole warp
-  constexpr bool GK = KT == KS_GAUSSIAN || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH;
+  constexpr bool GK = KT == KS_GAUSSIAN || KT == KS_GAUSSIAN_VAR_BANDWIDTH;
   uint32_t fl32 = 0;
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
   double rchk = 0.0;
@@ -1328,7 +1316,7 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   // it may flag pairs)
   const bool ffp = a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag);
   // columns per TMEM load: 8 for the kernels with the most live state per column
-  constexpr int NCH = (KT == KS_LAPLACE || KT == KS_GAUSS_UNSCALED || KT == KS_GAUSSIAN_VAR_BANDWIDTH) ? 8 : 16;
+  constexpr int NCH = (KT == KS_LAPLACE || KT == KS_GAUSSIAN_VAR_BANDWIDTH) ? 8 : 16;
 #pragma unroll 1
   for (int part = 0; part < 32 / NCH; part++) {
     const int c0 = grp * 32 + part * NCH;
@@ -1958,7 +1946,7 @@ __global__ void __launch_bounds__(256) list_rescue(TileArgs a, int ntask, const 
     double r = 0.0;
     for (int j = G.b0 + lane; j < G.b0 + G.n; j += 32) {
       switch (T.kp.type) {
-        case KS_GAUSSIAN: r += recheck<KS_GAUSS_UNSCALED, true>(a, T, ltab, pos, j); break;
+        case KS_GAUSSIAN: r += recheck<KS_GAUSSIAN, true>(a, T, ltab, pos, j); break;
         case KS_GAUSSIAN_VAR_BANDWIDTH: r += recheck<KS_GAUSSIAN_VAR_BANDWIDTH, true>(a, T, ltab, pos, j); break;
         default: r += recheck<KS_LAPLACE, true>(a, T, ltab, pos, j); break;
       }
