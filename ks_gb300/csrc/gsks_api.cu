@@ -174,10 +174,6 @@ int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
 {
   const bool norms = kt_uses_norms(ker->type);
   const bool varbw = ker->type == KS_GAUSSIAN_VAR_BANDWIDTH;
-  for (int i = 0; i < m; i++)
-    if (amap[i] < 0 || umap[i] < 0) return GSKS_ERR_MAP_RANGE;
-  for (int j = 0; j < n; j++)
-    if (bmap[j] < 0 || wmap[j] < 0) return GSKS_ERR_MAP_RANGE;
   if (norms && (!XA2 || !XB2)) return GSKS_ERR_ARG;
 
   const size_t mk = (size_t)m * k, nk = (size_t)n * k;
@@ -197,32 +193,52 @@ int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
   double *hhi = (double *)c->hhi.p, *hhj = (double *)c->hhj.p;
   double *hu = (double *)c->hu.p, *hw = (double *)c->hw.p;
   const size_t rowb = (size_t)k * sizeof(double);
-
-  int nt = host_threads_for(mk);
-#pragma omp parallel for num_threads(nt) schedule(static)
-  for (int i = 0; i < m; i++) {
-    const int p = amap[i];
-    memcpy(hA + (size_t)i * k, XA + (size_t)p * k, rowb);
-    if (norms) hA2[i] = XA2[p];
-    if (varbw) hhi[i] = ker->hi[p];
-    hu[i] = u[umap[i]];
-  }
-  nt = host_threads_for(nk);
-#pragma omp parallel for num_threads(nt) schedule(static)
-  for (int j = 0; j < n; j++) {
-    const int p = bmap[j];
-    memcpy(hB + (size_t)j * k, XB + (size_t)p * k, rowb);
-    if (norms) hB2[j] = XB2[p];
-    if (varbw) hhj[j] = ker->hj[p];
-    hw[j] = w[wmap[j]];
-  }
-
   cudaStream_t s = c->stream;
+
+  // Gather the rows the maps name into the pinned buffers and copy them, in
+  // chunks: the calling thread issues a chunk's copy while the team gathers
+  // the next one.  Maps are checked as they are read.
+  const int nt = host_threads_for(std::max(mk, nk));
+  const int ch = std::max(1024, (int)((4u << 20) / std::max(rowb, (size_t)8)));   // rows per chunk (~4 MiB)
+  int bad = 0;
   cudaError_t e = cudaSuccess;
+#pragma omp parallel num_threads(nt)
+  {
+    for (int side = 0; side < 2; side++) {
+      const int cnt = side ? n : m;
+      const int *map = side ? bmap : amap, *vmap = side ? wmap : umap;
+      const double *X = side ? XB : XA, *X2 = side ? XB2 : XA2, *hv = side ? ker->hj : ker->hi;
+      const double *val = side ? w : u;
+      double *hX = side ? hB : hA, *hX2 = side ? hB2 : hA2, *hh = side ? hhj : hhi, *hval = side ? hw : hu;
+      for (int r0 = 0; r0 < cnt; r0 += ch) {
+        const int r1 = std::min(cnt, r0 + ch);
+#pragma omp for schedule(static)
+        for (int i = r0; i < r1; i++) {
+          const int p = map[i], q = vmap[i];
+          if (p < 0 || q < 0) {
+#pragma omp atomic write
+            bad = 1;
+            continue;
+          }
+          memcpy(hX + (size_t)i * k, X + (size_t)p * k, rowb);
+          if (norms) hX2[i] = X2[p];
+          if (varbw) hh[i] = hv[p];
+          hval[i] = val[q];
+        }
+        // (the loop's barrier: the chunk is complete)
+#pragma omp master
+        {
+          double *dX = (double *)(side ? c->dB.p : c->dA.p);
+          if (e == cudaSuccess)
+            e = cudaMemcpyAsync(dX + (size_t)r0 * k, hX + (size_t)r0 * k, (size_t)(r1 - r0) * rowb,
+                                cudaMemcpyHostToDevice, s);
+        }
+      }
+    }
+  }
+  if (bad) return GSKS_ERR_MAP_RANGE;
 #define GSKS_CP(dst, src, bytes) \
   if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s)
-  GSKS_CP(c->dA.p, hA, mk * 8);
-  GSKS_CP(c->dB.p, hB, nk * 8);
   GSKS_CP(c->du.p, hu, (size_t)m * 8);
   GSKS_CP(c->dw.p, hw, (size_t)n * 8);
   if (norms) { GSKS_CP(c->dA2.p, hA2, (size_t)m * 8); GSKS_CP(c->dB2.p, hB2, (size_t)n * 8); }
