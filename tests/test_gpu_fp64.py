@@ -147,3 +147,25 @@ def test_device_map_range_flag(gpu):
     torch.cuda.synchronize()
     assert gsks.device_errors() & 1
     assert gsks.device_errors() == 0
+
+
+@pytest.mark.parametrize("which", ["amap", "umap", "bmap", "wmap"])
+def test_host_map_negative_index_refused(gpu, which):
+    """Host arrays: a negative index in any map returns GSKS_ERR_MAP_RANGE and
+    leaves u unchanged (the maps are checked while the rows are gathered, large
+    enough here for several gather chunks)."""
+    from ks_gb300 import gsks
+    X, X2, w, amap, bmap, umap, wmap = _random_case(12, 40000, 64, 20000, 20000)
+    maps = dict(amap=amap, umap=umap, bmap=bmap, wmap=wmap)
+    maps[which][17000] = -3
+    u = np.full(40000, 2.5)
+    for prec in (gsks.GSKS_FP64, gsks.GSKS_SPLIT_BF16X3):
+        prev = gsks.get_precision()
+        gsks.set_precision(prec)
+        try:
+            rc = gsks.dgsks_status(gsks.make_kernel(0, scal=-0.5), u, maps["umap"], X, X2, maps["amap"], X, X2,
+                                   maps["bmap"], w, maps["wmap"])
+        finally:
+            gsks.set_precision(prev)
+        assert rc == 5, gsks.error_string(rc)
+        assert np.all(u == 2.5)

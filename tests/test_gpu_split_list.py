@@ -138,3 +138,53 @@ def test_split_list_log_uniform_sizes(gpu, oracle_mod, k):
     specs = _specs(rng, ntask, k, kinds)
     _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True)
     assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+def test_split_list_rows_below_fp32_range(gpu, oracle_mod):
+    """Tasks whose targets lie far from their sources under a narrow Gaussian
+    (every value below the FP32 range, nonzero in FP64) beside ordinary tasks:
+    such task rows are redone in full after the chunk sums (list_rescue); the
+    others keep their FP32 sums."""
+    O = oracle_mod
+    rng = np.random.default_rng(31)
+    k, half = 3, 3000
+    X = np.empty((2 * half, k))
+    X[:half] = rng.uniform(0.0, 0.1, (half, k))          # sources
+    X[half:] = rng.uniform(1.4, 1.5, (half, k))          # far targets
+    w = rng.standard_normal(2 * half)
+    ntask = 12
+    sa = rng.integers(100, 900, ntask); sb = rng.integers(100, 1500, ntask)
+    a_parts, b_parts, specs = [], [], []
+    for t in range(ntask):
+        far = t % 2 == 0
+        pool_a = half + rng.permutation(half) if far else rng.permutation(half)
+        a_parts.append(pool_a[:sa[t]])
+        b_parts.append(rng.permutation(half)[:sb[t]])
+        if t % 4 == 0:
+            specs.append((0, dict(scal=-60.0)))          # far: K between 2^-585 and 2^-439
+        elif t % 4 == 2:
+            specs.append((2, {}))                        # far Laplace: ordinary values
+        else:
+            specs.append((0, dict(scal=-1.0 / (2 * rng.uniform(0.1, 2.0) ** 2))))
+    a_idx = np.concatenate(a_parts).astype(np.int32); b_idx = np.concatenate(b_parts).astype(np.int32)
+    a_off = np.concatenate([[0], np.cumsum(sa)]).astype(np.int32)
+    b_off = np.concatenate([[0], np.cumsum(sb)]).astype(np.int32)
+    u_idx = a_idx.copy(); w_idx = b_idx.copy()
+    _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+def test_split_list_more_items_than_ctas_of_uneven_cost(gpu, oracle_mod):
+    """Many small tasks and a few large ones: items of very different cost taken
+    from the work counter by 152 CTAs."""
+    O = oracle_mod
+    rng = np.random.default_rng(32)
+    N, k, ntask = 30000, 8, 400
+    X = rng.random((N, k)); w = rng.standard_normal(N)
+    sa = rng.integers(1, 40, ntask); sb = rng.integers(1, 60, ntask)
+    sa[:3] = 3000; sb[:3] = 4000
+    a_off, a_idx, b_off, b_idx = _lists(rng, N, sa, sb)
+    u_idx = a_idx.copy(); w_idx = b_idx.copy()
+    specs = _specs(rng, ntask, k, ["gauss", "laplace", "poly"])
+    _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
