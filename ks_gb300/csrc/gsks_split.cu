@@ -1297,7 +1297,7 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 // value of the 32 columns lies below 2^-96.  The 32 columns are summed in FP32 (four
 // interleaved partial sums) and enter the FP64 row sum with one conversion and
 // one add: FP64 instructions issue at a small fraction of the FP32 rate here.
-template <int KT>
+template <int KT, bool LISTED = false>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
                                               const SrcMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
                                               bool gfast, bool dump, const LTab &ltab, double &racc,
@@ -1315,8 +1315,9 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   // float-pair copies of the pools exist (a single call builds them only when
   // it may flag pairs)
   const bool ffp = a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag);
-  // columns per TMEM load: 8 for the kernels with the most live state per column
-  constexpr int NCH = (KT == KS_LAPLACE || KT == KS_GAUSSIAN_VAR_BANDWIDTH) ? 8 : 16;
+  // columns per TMEM load: 8 for the kernels with the most live state per column (the list
+  // form's Laplace too: its kernel holds every epilogue variant)
+  constexpr int NCH = (KT == KS_GAUSSIAN_VAR_BANDWIDTH || (KT == KS_LAPLACE && LISTED)) ? 8 : 16;
 #pragma unroll 1
   for (int part = 0; part < 32 / NCH; part++) {
     const int c0 = grp * 32 + part * NCH;
@@ -1609,7 +1610,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
             case KS_POLYNOMIAL:
               tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_LAPLACE, true>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             case KS_TANH:
               tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
             case KS_QUARTIC:
