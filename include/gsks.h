@@ -83,6 +83,27 @@ int gsks_dgsks_device(ks_t *kernel, int m, int n, int k,
                       const double *w, const int *wmap,
                       int precision, void *stream);
 
+/* Several right-hand sides.  u and w hold nrhs interleaved columns, the layout
+ * the reference's weighted sums use when built with KS_RHS = nrhs
+ * (include/ks.h:46):
+ *     u[umap[i]*nrhs + r] += sum_j K(XA[amap[i]], XB[bmap[j]]) w[wmap[j]*nrhs + r].
+ * Right-hand side r is one evaluation with the maps umap*nrhs + r and
+ * wmap*nrhs + r; the kernel values are evaluated again for every r.  The
+ * host-pointer form stages the points once for all r.  dgsks_rhs: host or
+ * device arrays, synchronous, as dgsks_status; gsks_dgsks_device_rhs: device
+ * arrays on `stream`, as gsks_dgsks_device. */
+int dgsks_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
+              double *u, int *umap,
+              double *XA, double *XA2, int *amap,
+              double *XB, double *XB2, int *bmap,
+              double *w, int *wmap);
+int gsks_dgsks_device_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
+                          double *u, const int *umap,
+                          const double *XA, const double *XA2, const int *amap, int nxa,
+                          const double *XB, const double *XB2, const int *bmap, int nxb,
+                          const double *w, const int *wmap,
+                          int precision, void *stream);
+
 /* gsks_dgsks_device() for callers that cannot let a library allocate device
  * memory -- e.g. a process whose device memory is reserved up front by its
  * own pool allocator, or a loop that may not allocate after start-up.  No

@@ -170,16 +170,18 @@ int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
                const double *u, const int *umap,
                const double *XA, const double *XA2, const int *amap,
                const double *XB, const double *XB2, const int *bmap,
-               const double *w, const int *wmap, Staged &v)
+               const double *w, const int *wmap, Staged &v, int nrhs)
 {
   const bool norms = kt_uses_norms(ker->type);
   const bool varbw = ker->type == KS_GAUSSIAN_VAR_BANDWIDTH;
   if (norms && (!XA2 || !XB2)) return GSKS_ERR_ARG;
 
   const size_t mk = (size_t)m * k, nk = (size_t)n * k;
-  bool ok = c->hA.ensure(mk * 8) && c->hB.ensure(nk * 8) && c->hu.ensure((size_t)m * 8) &&
-            c->hw.ensure((size_t)n * 8) && c->dA.ensure(mk * 8) && c->dB.ensure(nk * 8) &&
-            c->du.ensure((size_t)m * 8) && c->dw.ensure((size_t)n * 8);
+  // u and w keep their nrhs interleaved columns (u[umap[i] * nrhs + r])
+  const size_t R = (size_t)std::max(nrhs, 1);
+  bool ok = c->hA.ensure(mk * 8) && c->hB.ensure(nk * 8) && c->hu.ensure((size_t)m * R * 8) &&
+            c->hw.ensure((size_t)n * R * 8) && c->dA.ensure(mk * 8) && c->dB.ensure(nk * 8) &&
+            c->du.ensure((size_t)m * R * 8) && c->dw.ensure((size_t)n * R * 8);
   if (ok && norms)
     ok = c->hA2.ensure((size_t)m * 8) && c->hB2.ensure((size_t)n * 8) &&
          c->dA2.ensure((size_t)m * 8) && c->dB2.ensure((size_t)n * 8);
@@ -223,7 +225,7 @@ int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
           memcpy(hX + (size_t)i * k, X + (size_t)p * k, rowb);
           if (norms) hX2[i] = X2[p];
           if (varbw) hh[i] = hv[p];
-          hval[i] = val[q];
+          for (size_t r = 0; r < R; r++) hval[(size_t)i * R + r] = val[(size_t)q * R + r];
         }
         // (the loop's barrier: the chunk is complete)
 #pragma omp master
@@ -239,8 +241,8 @@ int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
   if (bad) return GSKS_ERR_MAP_RANGE;
 #define GSKS_CP(dst, src, bytes) \
   if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s)
-  GSKS_CP(c->du.p, hu, (size_t)m * 8);
-  GSKS_CP(c->dw.p, hw, (size_t)n * 8);
+  GSKS_CP(c->du.p, hu, (size_t)m * R * 8);
+  GSKS_CP(c->dw.p, hw, (size_t)n * R * 8);
   if (norms) { GSKS_CP(c->dA2.p, hA2, (size_t)m * 8); GSKS_CP(c->dB2.p, hB2, (size_t)n * 8); }
   if (varbw) { GSKS_CP(c->dhi.p, hhi, (size_t)m * 8); GSKS_CP(c->dhj.p, hhj, (size_t)n * 8); }
 #undef GSKS_CP
@@ -256,13 +258,15 @@ int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
 }
 
 // Copy the evaluated u back and scatter it in target order.
-int unstage_host(Ctx *c, int m, double *u, const int *umap)
+int unstage_host(Ctx *c, int m, double *u, const int *umap, int nrhs)
 {
-  cudaError_t e = cudaMemcpyAsync(c->hu.p, c->du.p, (size_t)m * 8, cudaMemcpyDeviceToHost, c->stream);
+  const size_t R = (size_t)std::max(nrhs, 1);
+  cudaError_t e = cudaMemcpyAsync(c->hu.p, c->du.p, (size_t)m * R * 8, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_status(e, "unstage_host");
   const double *hu = (const double *)c->hu.p;
-  for (int i = 0; i < m; i++) u[umap[i]] = hu[i];
+  for (int i = 0; i < m; i++)
+    for (size_t r = 0; r < R; r++) u[(size_t)umap[i] * R + r] = hu[(size_t)i * R + r];
   return GSKS_OK;
 }
 
@@ -333,6 +337,51 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
   if (e != cudaSuccess) return cuda_status(e, "fp64 launch");
   note_launches(launches);
   return GSKS_OK;
+}
+
+// ---- several right-hand sides -------------------------------------------
+// u and w hold nrhs interleaved columns, as the reference lays them out for
+// KS_RHS > 1 (u[umap[i] * KS_RHS + r], w[wmap[j] * KS_RHS + r]).  Right-hand
+// side r is one evaluation with the maps umap[i] * nrhs + r and
+// wmap[j] * nrhs + r, built on the device; the kernel values are evaluated
+// again for every r.
+__global__ void rhs_map_kernel(int cnt, const int *__restrict__ map, int nrhs, int r, int *__restrict__ out)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cnt) out[i] = (map ? map[i] : i) * nrhs + r;
+}
+
+int enqueue_rhs(Ctx *c, const ks_t *ker, int m, int n, int k, int nrhs, double *u, const int *umap,
+                const double *XA, const double *XA2, const int *amap, int nxa,
+                const double *XB, const double *XB2, const int *bmap, int nxb,
+                const double *w, const int *wmap, const double *hi, const double *hj,
+                int precision, cudaStream_t s, bool stream_ordered_alloc)
+{
+  if (nrhs == 1)
+    return enqueue_fused(c, ker, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb, w, wmap, hi, hj,
+                         precision, s, stream_ordered_alloc);
+  const size_t bytes = ((size_t)m + n) * sizeof(int);
+  int *maps = nullptr;
+  if (stream_ordered_alloc) {
+    const cudaError_t e = cudaMallocAsync((void **)&maps, bytes, s);
+    if (e != cudaSuccess) return cuda_status(e, "rhs maps");
+  } else {
+    if (!c->rmaps.ensure(bytes)) return GSKS_ERR_ALLOC;
+    maps = (int *)c->rmaps.p;
+  }
+  int st = GSKS_OK, launches = 0;
+  for (int r = 0; r < nrhs && st == GSKS_OK; r++) {
+    rhs_map_kernel<<<(m + 255) / 256, 256, 0, s>>>(m, umap, nrhs, r, maps);
+    rhs_map_kernel<<<(n + 255) / 256, 256, 0, s>>>(n, wmap, nrhs, r, maps + m);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { st = cuda_status(e, "rhs maps"); break; }
+    st = enqueue_fused(c, ker, m, n, k, u, maps, XA, XA2, amap, nxa, XB, XB2, bmap, nxb, w, maps + m, hi, hj,
+                       precision, s, stream_ordered_alloc);
+    launches += 2 + tl_launches;
+  }
+  if (stream_ordered_alloc) cudaFreeAsync(maps, s);
+  tl_launches = launches;
+  return st;
 }
 
 }  // namespace gsks
@@ -449,6 +498,61 @@ int gsks_dgsks_device(ks_t *kernel, int m, int n, int k,
   st = enqueue_fused(c, kernel, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb,
                      w, wmap, kernel->hi, kernel->hj, precision, (cudaStream_t)stream, true);
   return set_status(st, "gsks_dgsks_device");
+}
+
+int gsks_dgsks_device_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
+                          double *u, const int *umap,
+                          const double *XA, const double *XA2, const int *amap, int nxa,
+                          const double *XB, const double *XB2, const int *bmap, int nxb,
+                          const double *w, const int *wmap,
+                          int precision, void *stream)
+{
+  tl_launches = 0;
+  if (m < 0 || n < 0 || k < 0 || nrhs < 1) return set_status(GSKS_ERR_ARG, "gsks_dgsks_device_rhs");
+  if (m == 0 || n == 0 || k == 0) return set_status(GSKS_OK, nullptr);
+  int st = check_kernel(kernel, k);
+  if (st) return set_status(st, "gsks_dgsks_device_rhs");
+  if (!u || !XA || !XB || !w) return set_status(GSKS_ERR_ARG, "gsks_dgsks_device_rhs");
+  if (kt_uses_norms(kernel->type) && (!XA2 || !XB2))
+    return set_status(GSKS_ERR_ARG, "gsks_dgsks_device_rhs");
+  Ctx *c = get_ctx();
+  if (!c) return tl_status;
+  st = enqueue_rhs(c, kernel, m, n, k, nrhs, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb,
+                   w, wmap, kernel->hi, kernel->hj, precision, (cudaStream_t)stream, true);
+  return set_status(st, "gsks_dgsks_device_rhs");
+}
+
+int dgsks_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
+              double *u, int *umap,
+              double *XA, double *XA2, int *amap,
+              double *XB, double *XB2, int *bmap,
+              double *w, int *wmap)
+{
+  tl_launches = 0;
+  if (m < 0 || n < 0 || k < 0 || nrhs < 1) return set_status(GSKS_ERR_ARG, "dgsks_rhs");
+  if (m == 0 || n == 0 || k == 0) return set_status(GSKS_OK, nullptr);
+  int st = check_kernel(kernel, k);
+  if (st) return set_status(st, "dgsks_rhs");
+  if (!u || !umap || !XA || !amap || !XB || !bmap || !w || !wmap) return set_status(GSKS_ERR_ARG, "dgsks_rhs");
+  Ctx *c = get_ctx();
+  if (!c) return tl_status;
+  const int prec = effective_precision();
+  if (is_device_pointer(XA)) {
+    st = enqueue_rhs(c, kernel, m, n, k, nrhs, u, umap, XA, XA2, amap, -1, XB, XB2, bmap, -1, w, wmap,
+                     kernel->hi, kernel->hj, prec, c->stream, false);
+    if (st) return set_status(st, "dgsks_rhs");
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_status(e, "dgsks_rhs");
+    return set_status(GSKS_OK, nullptr);
+  }
+  Staged v;
+  st = stage_host(c, kernel, m, n, k, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap, v, nrhs);
+  if (st) return set_status(st, "dgsks_rhs");
+  st = enqueue_rhs(c, kernel, m, n, k, nrhs, v.u, nullptr, v.A, v.A2, nullptr, m, v.B, v.B2, nullptr, n, v.w,
+                   nullptr, v.hi, v.hj, prec, c->stream, false);
+  if (st) return set_status(st, "dgsks_rhs");
+  st = unstage_host(c, m, u, umap, nrhs);
+  return set_status(st, "dgsks_rhs");
 }
 
 int gsks_norms_device(int N, int k, const double *X, double *X2, void *stream)

@@ -29,6 +29,7 @@ struct Ctx {
   int num_sms = 0;
   DevBuf partial, err;
   DevBuf dA, dA2, dB, dB2, dw, du, dhi, dhj, dwork;
+  DevBuf rmaps;                // per-rhs u and w maps of the multi-rhs calls
   PinBuf hA, hA2, hB, hB2, hw, hu, hhi, hhj;
   ~Ctx();
 };
@@ -55,8 +56,8 @@ int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
                const double *u, const int *umap,
                const double *XA, const double *XA2, const int *amap,
                const double *XB, const double *XB2, const int *bmap,
-               const double *w, const int *wmap, Staged &v);
-int unstage_host(Ctx *c, int m, double *u, const int *umap);
+               const double *w, const int *wmap, Staged &v, int nrhs = 1);
+int unstage_host(Ctx *c, int m, double *u, const int *umap, int nrhs = 1);
 
 int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
                   double *u, const int *umap,

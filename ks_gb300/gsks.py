@@ -64,6 +64,10 @@ def load():
     lib.gsks_dgsks_device.restype = C.c_int
     lib.gsks_dgsks_device.argtypes = [C.POINTER(KsT), ip, ip, ip, vp, vp, vp, vp, vp, ip,
                                       vp, vp, vp, ip, vp, vp, ip, vp]
+    lib.gsks_dgsks_device_rhs.restype = C.c_int
+    lib.gsks_dgsks_device_rhs.argtypes = [C.POINTER(KsT), ip, ip, ip, ip, vp, vp, vp, vp, vp, ip,
+                                          vp, vp, vp, ip, vp, vp, ip, vp]
+    lib.dgsks_rhs.restype = C.c_int
     lib.gsks_norms_device.restype = C.c_int
     lib.gsks_norms_device.argtypes = [ip, ip, vp, vp, vp]
     lib.gsks_error_string.restype = C.c_char_p
@@ -181,6 +185,29 @@ def dgsks_device(ker: KsT, m, n, k, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wm
         _addr(XB), _addr(XB2), _addr(bmap), nxb, _addr(w), _addr(wmap), int(precision), s)
     if rc:
         raise GsksError(rc, "gsks_dgsks_device")
+
+
+def dgsks_device_rhs(ker: KsT, m, n, k, nrhs, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap,
+                     precision=GSKS_FP64, stream=None, nxa=-1, nxb=-1) -> None:
+    """dgsks_device with nrhs interleaved right-hand sides:
+    u[umap[i]*nrhs + r] += sum_j K_ij w[wmap[j]*nrhs + r]."""
+    s = stream if isinstance(stream, int) or stream is None else stream.cuda_stream
+    rc = load().gsks_dgsks_device_rhs(
+        C.byref(ker), m, n, k, int(nrhs), _addr(u), _addr(umap), _addr(XA), _addr(XA2), _addr(amap), nxa,
+        _addr(XB), _addr(XB2), _addr(bmap), nxb, _addr(w), _addr(wmap), int(precision), s)
+    if rc:
+        raise GsksError(rc, "gsks_dgsks_device_rhs")
+
+
+def dgsks_rhs(ker: KsT, nrhs, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap, k=None) -> int:
+    """Synchronous multi-rhs call (gsks.h dgsks_rhs); host or device arrays; the status."""
+    m = int(amap.numel() if hasattr(amap, "numel") else amap.size)
+    n = int(bmap.numel() if hasattr(bmap, "numel") else bmap.size)
+    if k is None:
+        k = int(XA.shape[1])
+    return int(load().dgsks_rhs(
+        C.byref(ker), C.c_int(m), C.c_int(n), C.c_int(k), C.c_int(int(nrhs)), _vp(u), _vp(umap), _vp(XA),
+        _vp(XA2), _vp(amap), _vp(XB), _vp(XB2), _vp(bmap), _vp(w), _vp(wmap)))
 
 
 def norms_device(X, X2, stream=None) -> None:
