@@ -390,11 +390,44 @@ def run_ours(args, ws, rank, local):
         line["error"] = err
     if not args.no_e2e:
         line["e2e"] = run_e2e(args, torch, gsks, wl, ws, head)
+    if ws == 1 and head == "split":
+        line["rhs"] = run_rhs(args, torch, gsks, wl, stream)
     if not args.no_list and ws == 1:
         del wl
         torch.cuda.empty_cache()
         line["list"] = run_list(args, torch, gsks, forms)
     return line
+
+
+def run_rhs(args, torch, gsks, wl, stream, nrhs=4):
+    """Several right-hand sides (gsks_dgsks_device_rhs): the Gaussian of the
+    step over the same pairs with nrhs interleaved weight columns, split form,
+    device-resident; pair-evals/s counts one per pair and right-hand side."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(99)
+    w = torch.randn(N_S * nrhs, dtype=torch.float64, device="cuda", generator=g)
+    u = torch.zeros(M_T * nrhs, dtype=torch.float64, device="cuda")
+    name, kt, p, _ = KERNELS[0]
+    ker = gsks.make_kernel(kt, **p)
+    call = lambda: gsks.dgsks_device_rhs(ker, M_T, N_S, K_DIM, nrhs, u, wl["umap"], wl["X"], wl["X2"], wl["amap"],
+                                         wl["X"], wl["X2"], wl["bmap"], w, wl["wmap"],
+                                         precision=gsks.GSKS_SPLIT_BF16X3, stream=stream, nxa=N_POOL, nxb=N_POOL)
+    for _ in range(max(1, args.warmup)):
+        call()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    ts = []
+    for _ in range(max(1, args.steps)):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        call()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    ms = statistics.median(ts)
+    return {"kernel": name, "nrhs": nrhs, "ms": round(ms, 3), "value": float(M_T) * N_S * nrhs / (ms * 1e-3),
+            "unit": "pair-evals/s (per right-hand side)", "form": "split",
+            "note": "one sweep per right-hand side (the kernel values are evaluated again for each)"}
 
 
 def make_list_workload(ntask=LIST_TASKS, seed=4321):
