@@ -104,6 +104,25 @@ int gsks_dgsks_device_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
                           const double *w, const int *wmap,
                           int precision, void *stream);
 
+/* Single precision: dgsks on FP32 arrays (host or device, synchronous).  The
+ * reference declares no such entry; its single-precision micro-kernels are
+ * stubs.  The rows the maps name are converted to FP64 as they are gathered,
+ * and XA2/XB2 are recomputed in FP64 from them (the arguments are accepted and
+ * ignored).  The evaluation is dgsks's, in the precision of
+ * gsks_set_precision(), and u[umap[i]] is written back rounded to FP32.  The
+ * bandwidth vectors of the variable-bandwidth kernel stay FP64 (ks_t).
+ * sgsks_status returns the status; sgsks is void like dgsks. */
+int sgsks_status(ks_t *kernel, int m, int n, int k,
+                 float *u, int *umap,
+                 float *XA, float *XA2, int *amap,
+                 float *XB, float *XB2, int *bmap,
+                 float *w, int *wmap);
+void sgsks(ks_t *kernel, int m, int n, int k,
+           float *u, int *umap,
+           float *XA, float *XA2, int *amap,
+           float *XB, float *XB2, int *bmap,
+           float *w, int *wmap);
+
 /* gsks_dgsks_device() for callers that cannot let a library allocate device
  * memory -- e.g. a process whose device memory is reserved up front by its
  * own pool allocator, or a loop that may not allocate after start-up.  No

@@ -68,6 +68,7 @@ def load():
     lib.gsks_dgsks_device_rhs.argtypes = [C.POINTER(KsT), ip, ip, ip, ip, vp, vp, vp, vp, vp, ip,
                                           vp, vp, vp, ip, vp, vp, ip, vp]
     lib.dgsks_rhs.restype = C.c_int
+    lib.sgsks_status.restype = C.c_int
     lib.gsks_norms_device.restype = C.c_int
     lib.gsks_norms_device.argtypes = [ip, ip, vp, vp, vp]
     lib.gsks_error_string.restype = C.c_char_p
@@ -160,6 +161,18 @@ def dgsks_status(ker: KsT, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap, k=Non
     if k is None:
         k = int(XA.shape[1])
     return int(load().dgsks_status(
+        C.byref(ker), C.c_int(m), C.c_int(n), C.c_int(k), _vp(u), _vp(umap), _vp(XA), _vp(XA2),
+        _vp(amap), _vp(XB), _vp(XB2), _vp(bmap), _vp(w), _vp(wmap)))
+
+
+def sgsks_status(ker: KsT, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap, k=None) -> int:
+    """Single precision (gsks.h sgsks_status): FP32 u, XA, XB, w (host or device);
+    XA2/XB2 may be None (recomputed in FP64).  Returns the status."""
+    m = int(amap.numel() if hasattr(amap, "numel") else amap.size)
+    n = int(bmap.numel() if hasattr(bmap, "numel") else bmap.size)
+    if k is None:
+        k = int(XA.shape[1])
+    return int(load().sgsks_status(
         C.byref(ker), C.c_int(m), C.c_int(n), C.c_int(k), _vp(u), _vp(umap), _vp(XA), _vp(XA2),
         _vp(amap), _vp(XB), _vp(XB2), _vp(bmap), _vp(w), _vp(wmap)))
 
