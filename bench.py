@@ -425,9 +425,33 @@ def run_rhs(args, torch, gsks, wl, stream, nrhs=4):
         torch.cuda.synchronize()
         ts.append(a.elapsed_time(b))
     ms = statistics.median(ts)
-    return {"kernel": name, "nrhs": nrhs, "ms": round(ms, 3), "value": float(M_T) * N_S * nrhs / (ms * 1e-3),
-            "unit": "pair-evals/s (per right-hand side)", "form": "split",
-            "note": "one sweep per right-hand side (the kernel values are evaluated again for each)"}
+    out = {"kernel": name, "nrhs": nrhs, "ms": round(ms, 3), "value": float(M_T) * N_S * nrhs / (ms * 1e-3),
+           "unit": "pair-evals/s (per right-hand side)", "form": "split",
+           "note": "split form: one sweep per right-hand side (the kernel values are evaluated again for each)"}
+    # FP64 form on a block of 8192 target rows: nrhs right-hand sides in one
+    # pass (each kernel value formed once) against one right-hand side
+    mr = 8192
+    rows = wl["amap"][:mr]
+    urow = torch.arange(mr, dtype=torch.int32, device="cuda")
+    ub = torch.zeros(mr * nrhs, dtype=torch.float64, device="cuda")
+
+    def fp64(r):
+        gsks.dgsks_device_rhs(ker, mr, N_S, K_DIM, r, ub, urow, wl["X"], wl["X2"], rows, wl["X"], wl["X2"],
+                              wl["bmap"], w, wl["wmap"], precision=gsks.GSKS_FP64, stream=stream,
+                              nxa=N_POOL, nxb=N_POOL)
+
+    for r in (1, nrhs):
+        fp64(r)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fp64(r)
+        b.record(stream)
+        torch.cuda.synchronize()
+        out[f"fp64_ms_rows{mr}_nrhs{r}"] = round(a.elapsed_time(b), 3)
+    out["fp64_note"] = (f"FP64 form, {mr} target rows: {nrhs} right-hand sides in one pass against one; "
+                        "w read with stride nrhs in both")
+    return out
 
 
 def make_list_workload(ntask=LIST_TASKS, seed=4321):

@@ -87,9 +87,11 @@ int gsks_dgsks_device(ks_t *kernel, int m, int n, int k,
  * the reference's weighted sums use when built with KS_RHS = nrhs
  * (include/ks.h:46):
  *     u[umap[i]*nrhs + r] += sum_j K(XA[amap[i]], XB[bmap[j]]) w[wmap[j]*nrhs + r].
- * Right-hand side r is one evaluation with the maps umap*nrhs + r and
- * wmap*nrhs + r; the kernel values are evaluated again for every r.  The
- * host-pointer form stages the points once for all r.  dgsks_rhs: host or
+ * The FP64 form takes up to four right-hand sides in one pass, each kernel
+ * value multiplied by every weight column.  Otherwise (the split form, or
+ * nrhs > 4) right-hand side r is one evaluation with the maps umap*nrhs + r
+ * and wmap*nrhs + r, and the kernel values are evaluated again for every r.
+ * The host-pointer form stages the points once for all r.  dgsks_rhs: host or
  * device arrays, synchronous, as dgsks_status; gsks_dgsks_device_rhs: device
  * arrays on `stream`, as gsks_dgsks_device. */
 int dgsks_rhs(ks_t *kernel, int m, int n, int k, int nrhs,

@@ -304,20 +304,23 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
                   const double *XA, const double *XA2, const int *amap, int nxa,
                   const double *XB, const double *XB2, const int *bmap, int nxb,
                   const double *w, const int *wmap, const double *hi, const double *hj,
-                  int precision, cudaStream_t s, bool stream_ordered_alloc)
+                  int precision, cudaStream_t s, bool stream_ordered_alloc, int nrhs)
 {
+  // nrhs > 1: FP64 form only (interleaved u and w, each K formed once)
+  if (nrhs > 1 && precision != GSKS_FP64) return GSKS_ERR_ARG;
   if (precision == GSKS_SPLIT_BF16X3)
     return enqueue_split(c, ker, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb,
                          w, wmap, hi, hj, s, stream_ordered_alloc);
   if (precision != GSKS_FP64) return GSKS_ERR_PRECISION;
 
   Fp64Plan p = fp64_plan(m, n, k, c->num_sms);
+  const size_t pbytes = p.partial_elems * sizeof(double) * (size_t)std::max(nrhs, 1);
   double *partial = nullptr;
   if (stream_ordered_alloc) {
-    cudaError_t e = cudaMallocAsync((void **)&partial, p.partial_elems * sizeof(double), s);
+    cudaError_t e = cudaMallocAsync((void **)&partial, pbytes, s);
     if (e != cudaSuccess) return cuda_status(e, "cudaMallocAsync");
   } else {
-    if (!c->partial.ensure(p.partial_elems * sizeof(double))) return GSKS_ERR_ALLOC;
+    if (!c->partial.ensure(pbytes)) return GSKS_ERR_ALLOC;
     partial = (double *)c->partial.p;
   }
   FusedArgs a{};
@@ -330,6 +333,7 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
   a.nxa = nxa; a.nxb = nxb;
   a.partial = partial;
   a.err = (int *)c->err.p;
+  a.nrhs = std::max(nrhs, 1);
   int launches = fp64_launch(a, p, u, umap, s);
   if (launches < 0) return GSKS_ERR_KERNEL_TYPE;
   cudaError_t e = cudaGetLastError();
@@ -341,10 +345,11 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
 
 // ---- several right-hand sides -------------------------------------------
 // u and w hold nrhs interleaved columns, as the reference lays them out for
-// KS_RHS > 1 (u[umap[i] * KS_RHS + r], w[wmap[j] * KS_RHS + r]).  Right-hand
-// side r is one evaluation with the maps umap[i] * nrhs + r and
-// wmap[j] * nrhs + r, built on the device; the kernel values are evaluated
-// again for every r.
+// KS_RHS > 1 (u[umap[i] * KS_RHS + r], w[wmap[j] * KS_RHS + r]).  The FP64
+// form takes up to four in one pass, each kernel value multiplied by every
+// weight column.  Otherwise right-hand side r is one evaluation with the maps
+// umap[i] * nrhs + r and wmap[j] * nrhs + r, built on the device, and the
+// kernel values are evaluated again for every r.
 __global__ void rhs_map_kernel(int cnt, const int *__restrict__ map, int nrhs, int r, int *__restrict__ out)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -357,9 +362,9 @@ int enqueue_rhs(Ctx *c, const ks_t *ker, int m, int n, int k, int nrhs, double *
                 const double *w, const int *wmap, const double *hi, const double *hj,
                 int precision, cudaStream_t s, bool stream_ordered_alloc)
 {
-  if (nrhs == 1)
+  if (nrhs == 1 || (precision == GSKS_FP64 && nrhs <= 4))   // one pass, each K formed once
     return enqueue_fused(c, ker, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb, w, wmap, hi, hj,
-                         precision, s, stream_ordered_alloc);
+                         precision, s, stream_ordered_alloc, nrhs);
   const size_t bytes = ((size_t)m + n) * sizeof(int);
   int *maps = nullptr;
   if (stream_ordered_alloc) {

@@ -25,7 +25,7 @@ namespace gsks {
 
 namespace {
 
-template <int KT>
+template <int KT, int R>
 __global__ void __launch_bounds__(fp64cfg::NT, 2) fp64_tiles(FusedArgs a)
 {
   __shared__ Fp64Smem sm;
@@ -35,21 +35,24 @@ __global__ void __launch_bounds__(fp64cfg::NT, 2) fp64_tiles(FusedArgs a)
     const int sc = item / a.ntm;
     const int i0 = ti * fp64cfg::BM;
     const int j0 = sc * a.chunk;
-    fp64_item<KT>(a, a.kp, sm, i0, min(fp64cfg::BM, a.m - i0), j0, min(a.chunk, a.n - j0),
-                  a.partial + (size_t)sc * a.ldp + i0);
+    fp64_item<KT, R>(a, a.kp, sm, i0, min(fp64cfg::BM, a.m - i0), j0, min(a.chunk, a.n - j0),
+                     a.partial + (size_t)sc * a.ldp + i0);
   }
 }
 
-// u[umap[i]] += sum over chunks of the chunk partials, in chunk order.
-__global__ void fp64_reduce(int m, int nsc, int ldp, const double *__restrict__ partial,
+// u[umap[i] R + q] += sum over chunks of the chunk partials of right-hand
+// side q, in chunk order.
+__global__ void fp64_reduce(int m, int nsc, int ldp, int R, long long rstride, const double *__restrict__ partial,
                             double *__restrict__ u, const int *__restrict__ umap)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
-  double s = 0.0;
-  for (int c = 0; c < nsc; c++) s += partial[(size_t)c * ldp + i];
-  const int p = umap ? umap[i] : i;
-  u[p] += s;
+  const size_t p = (size_t)(umap ? umap[i] : i) * R;
+  for (int q = 0; q < R; q++) {
+    double s = 0.0;
+    for (int c = 0; c < nsc; c++) s += partial[(size_t)q * rstride + (size_t)c * ldp + i];
+    u[p + q] += s;
+  }
 }
 
 // One warp per point: X2[p] = sum_q X[p*k+q]^2.
@@ -69,7 +72,12 @@ __global__ void norms_kernel(int N, int k, const double *__restrict__ X, double 
 template <int KT>
 void launch_tiles(const FusedArgs &a, int grid, cudaStream_t s)
 {
-  fp64_tiles<KT><<<grid, fp64cfg::NT, 0, s>>>(a);
+  switch (a.nrhs) {
+    case 2: fp64_tiles<KT, 2><<<grid, fp64cfg::NT, 0, s>>>(a); break;
+    case 3: fp64_tiles<KT, 3><<<grid, fp64cfg::NT, 0, s>>>(a); break;
+    case 4: fp64_tiles<KT, 4><<<grid, fp64cfg::NT, 0, s>>>(a); break;
+    default: fp64_tiles<KT, 1><<<grid, fp64cfg::NT, 0, s>>>(a); break;
+  }
 }
 }  // namespace
 
@@ -100,6 +108,8 @@ int fp64_launch(const FusedArgs &a0, const Fp64Plan &p, double *u, const int *um
 {
   FusedArgs a = a0;
   a.ntm = p.ntm; a.nsc = p.nsc; a.chunk = p.chunk; a.ldp = p.ldp;
+  if (a.nrhs < 1 || a.nrhs > fp64cfg::RMAX) a.nrhs = 1;
+  a.rstride = (long long)p.nsc * p.ldp;
   switch (a.kp.type) {
     case KS_GAUSSIAN: launch_tiles<KS_GAUSSIAN>(a, p.grid, s); break;
     case KS_POLYNOMIAL: launch_tiles<KS_POLYNOMIAL>(a, p.grid, s); break;
@@ -111,7 +121,7 @@ int fp64_launch(const FusedArgs &a0, const Fp64Plan &p, double *u, const int *um
     case KS_EPANECHNIKOV: launch_tiles<KS_EPANECHNIKOV>(a, p.grid, s); break;
     default: return -1;
   }
-  fp64_reduce<<<(a.m + 255) / 256, 256, 0, s>>>(a.m, p.nsc, p.ldp, a.partial, u, umap);
+  fp64_reduce<<<(a.m + 255) / 256, 256, 0, s>>>(a.m, p.nsc, p.ldp, a.nrhs, a.rstride, a.partial, u, umap);
   return 2;
 }
 

@@ -17,20 +17,23 @@ constexpr int BN = 64;    // sources per tile
 constexpr int KC = 16;    // k chunk staged in shared memory
 constexpr int NT = 256;   // threads per CTA
 constexpr int TM = 4, TN = 4;
+constexpr int RMAX = 4;   // right-hand sides evaluated together
 }  // namespace fp64cfg
 
 struct Fp64Smem {
   double As[fp64cfg::KC][fp64cfg::BM + 1];
   double Bs[fp64cfg::KC][fp64cfg::BN + 1];
   double aa[fp64cfg::BM], hi[fp64cfg::BM];
-  double bb[fp64cfg::BN], hj[fp64cfg::BN], w[fp64cfg::BN];
+  double bb[fp64cfg::BN], hj[fp64cfg::BN], w[fp64cfg::RMAX][fp64cfg::BN];
   long long arow[fp64cfg::BM], brow[fp64cfg::BN];
 };
 
 // Rows a0 .. a0+rows-1 of the call (positions in amap), sources b0 ..
 // b0+cols-1 (positions in bmap / wmap).  out[r] = sum_j K(r, j) w(j) for
-// r < rows.  Must be called by all NT threads of the block.
-template <int KT>
+// r < rows.  With R right-hand sides (w[wmap[j] R + q]) each K(r, j) is
+// formed once and out[q rstride + r] receives right-hand side q.  Must be
+// called by all NT threads of the block.
+template <int KT, int R = 1>
 __device__ __forceinline__ void fp64_item(const FusedArgs &a, const KParams &kp, Fp64Smem &sm,
                                           int a0, int rows, int b0, int cols, double *out)
 {
@@ -53,16 +56,20 @@ __device__ __forceinline__ void fp64_item(const FusedArgs &a, const KParams &kp,
     sm.arow[tid] = off; sm.aa[tid] = aav; sm.hi[tid] = hiv;
   }
 
-  double racc[TM];
+  double racc[TM][R];
 #pragma unroll
-  for (int r = 0; r < TM; r++) racc[r] = 0.0;
+  for (int r = 0; r < TM; r++)
+#pragma unroll
+    for (int q = 0; q < R; q++) racc[r][q] = 0.0;
 
   for (int j0 = 0; j0 < cols; j0 += BN) {
     const int ncols = min(BN, cols - j0);
     __syncthreads();  // the previous source tile's metadata is consumed
     if (tid < BN) {
       long long off = 0;
-      double bbv = 0.0, hjv = 0.0, wv = 0.0;
+      double bbv = 0.0, hjv = 0.0, wv[R];
+#pragma unroll
+      for (int q = 0; q < R; q++) wv[q] = 0.0;
       if (tid < ncols) {
         const int j = b0 + j0 + tid;
         int p = a.bmap ? __ldg(a.bmap + j) : j;
@@ -70,9 +77,13 @@ __device__ __forceinline__ void fp64_item(const FusedArgs &a, const KParams &kp,
         off = (long long)p * k;
         if (kt_uses_norms(KT)) bbv = __ldg(a.XB2 + p);
         if (KT == KS_GAUSSIAN_VAR_BANDWIDTH) hjv = __ldg(kp.hj + p);
-        wv = __ldg(a.w + (a.wmap ? __ldg(a.wmap + j) : j));
+        const size_t wj = (size_t)(a.wmap ? __ldg(a.wmap + j) : j) * R;
+#pragma unroll
+        for (int q = 0; q < R; q++) wv[q] = __ldg(a.w + wj + q);
       }
-      sm.brow[tid] = off; sm.bb[tid] = bbv; sm.hj[tid] = hjv; sm.w[tid] = wv;
+      sm.brow[tid] = off; sm.bb[tid] = bbv; sm.hj[tid] = hjv;
+#pragma unroll
+      for (int q = 0; q < R; q++) sm.w[q][tid] = wv[q];
     }
 
     double acc[TM][TN];
@@ -130,16 +141,20 @@ __device__ __forceinline__ void fp64_item(const FusedArgs &a, const KParams &kp,
     for (int r = 0; r < TM; r++) {
       const int rr = ty + 16 * r;
       const double aav = sm.aa[rr], hiv = sm.hi[rr];
-      double s = 0.0;
+      double s[R];
+#pragma unroll
+      for (int q = 0; q < R; q++) s[q] = 0.0;
 #pragma unroll
       for (int c = 0; c < TN; c++) {
         const int cc = tx + 16 * c;
         if (cc < ncols) {
           const double kv = kfun64<KT>(acc[r][c], aav, sm.bb[cc], hiv, sm.hj[cc], kp);
-          s = fma(kv, sm.w[cc], s);
+#pragma unroll
+          for (int q = 0; q < R; q++) s[q] = fma(kv, sm.w[q][cc], s[q]);
         }
       }
-      racc[r] += s;
+#pragma unroll
+      for (int q = 0; q < R; q++) racc[r][q] += s[q];
     }
   }
 
@@ -147,14 +162,19 @@ __device__ __forceinline__ void fp64_item(const FusedArgs &a, const KParams &kp,
 #pragma unroll
   for (int r = 0; r < TM; r++) {
 #pragma unroll
-    for (int off = 8; off > 0; off >>= 1)
-      racc[r] += __shfl_xor_sync(0xffffffffu, racc[r], off);
+    for (int q = 0; q < R; q++)
+#pragma unroll
+      for (int off = 8; off > 0; off >>= 1)
+        racc[r][q] += __shfl_xor_sync(0xffffffffu, racc[r][q], off);
   }
   if (tx == 0) {
 #pragma unroll
     for (int r = 0; r < TM; r++) {
       const int rr = ty + 16 * r;
-      if (rr < rows) out[rr] = racc[r];
+      if (rr < rows) {
+#pragma unroll
+        for (int q = 0; q < R; q++) out[(size_t)q * a.rstride + rr] = racc[r][q];
+      }
     }
   }
 }

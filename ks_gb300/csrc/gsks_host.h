@@ -64,7 +64,7 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
                   const double *XA, const double *XA2, const int *amap, int nxa,
                   const double *XB, const double *XB2, const int *bmap, int nxb,
                   const double *w, const int *wmap, const double *hi, const double *hj,
-                  int precision, cudaStream_t s, bool stream_ordered_alloc);
+                  int precision, cudaStream_t s, bool stream_ordered_alloc, int nrhs = 1);
 
 // Split-precision form (gsks_split.cu).
 int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k,

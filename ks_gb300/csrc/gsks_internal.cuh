@@ -78,9 +78,11 @@ struct FusedArgs {
   int ntm;                // number of target tiles
   int nsc;                // number of source chunks
   int chunk;              // sources per chunk (multiple of the source tile)
-  double *partial;        // [nsc][ldp] per-chunk row sums
+  double *partial;        // [nrhs][nsc][ldp] per-chunk row sums
   int ldp;
   int *err;               // device error flags
+  int nrhs;               // right-hand sides interleaved in u and w (0 or 1: one)
+  long long rstride;      // partial elements per right-hand side
 };
 
 // ---------------------------------------------------------------------------
