@@ -79,7 +79,7 @@ int sgsks_status(ks_t *kernel, int m, int n, int k,
   const size_t mk = (size_t)m * k, nk = (size_t)n * k;
   bool ok = c->dA.ensure(mk * 8) && c->dB.ensure(nk * 8) && c->dA2.ensure((size_t)m * 8) &&
             c->dB2.ensure((size_t)n * 8) && c->du.ensure((size_t)m * 8) && c->dw.ensure((size_t)n * 8) &&
-            c->err.ensure(sizeof(int));
+            c->rmaps.ensure(sizeof(int));
   if (ok && varbw) ok = c->dhi.ensure((size_t)m * 8) && c->dhj.ensure((size_t)n * 8);
   if (!ok) return set_status(GSKS_ERR_ALLOC, "sgsks");
   double *dA = (double *)c->dA.p, *dB = (double *)c->dB.p, *dA2 = (double *)c->dA2.p, *dB2 = (double *)c->dB2.p;
@@ -89,7 +89,7 @@ int sgsks_status(ks_t *kernel, int m, int n, int k,
   const int prec = effective_precision();
 
   if (is_device_pointer(XA)) {
-    int *bad = (int *)c->err.p;
+    int *bad = (int *)c->rmaps.p;   // its own flag: the context's error word keeps earlier calls' flags
     cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), s);
     const int blocks = std::max(1, std::min(1024, (std::max(m, n) + 7) / 8));
     gather_rows_f32<<<blocks, 256, 0, s>>>(m, k, XA, amap, varbw ? kernel->hi : nullptr, u, umap, dA, dA2, dhi, du,
