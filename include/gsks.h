@@ -39,7 +39,8 @@ enum {
   GSKS_ERR_LIST = 8,         /* inconsistent task lists                       */
   GSKS_ERR_PRECISION = 9,    /* unknown precision, or form not built          */
   GSKS_ERR_NO_DEVICE = 10,   /* no CUDA device visible                        */
-  GSKS_ERR_TOO_LARGE = 11    /* a size beyond what the entry point supports   */
+  GSKS_ERR_TOO_LARGE = 11,   /* a size beyond what the entry point supports   */
+  GSKS_ERR_TIMEOUT = 12      /* a kernel's bounded wait gave up: u incomplete */
 };
 
 /* Status of the calling thread's most recent GSKS call. */
@@ -50,8 +51,13 @@ const char *gsks_error_string(int code);
 /* ---- precision --------------------------------------------------------- */
 enum {
   GSKS_FP64 = 0,        /* FP64 rank-k, FP64 kernel function and sums        */
-  GSKS_SPLIT_BF16X3 = 1 /* split 3xBF16 tensor-core rank-k, FP32 kernel
-                           function, FP64 norms / near-pair distances / u    */
+  GSKS_SPLIT_BF16X3 = 1 /* split-precision tensor-core form.  (The name is
+                           kept for compatibility: each coordinate is split
+                           into three 16-bit slices, an integer head exact in
+                           FP16 and two FP16 remainders, multiplied with
+                           tcgen05 kind::f16 and FP32 accumulation.)  FP32
+                           kernel function; FP64 norms, near-pair distances
+                           and accumulation of u; <= 1e-6 relative error.   */
 };
 
 /* Precision used by dgsks()/dgsks_list() on the calling thread.  The
@@ -150,9 +156,14 @@ int gsks_norms_device(int N, int k, const double *X, double *X2, void *stream);
 int gsks_last_launch_count(void);
 
 /* Waits for the device, then returns and clears the device-side error flags
- * of the calling thread's context (bit 0: a map index outside [0, nxa/nxb)
- * was clamped and skipped by gsks_dgsks_device).  Returns -1 if the flags
- * could not be read. */
+ * of the calling thread's asynchronous calls (gsks_dgsks_device,
+ * gsks_dgsks_device_rhs).  Bit 0: a map index outside [0, nxa/nxb) was
+ * clamped and read as point 0.  Bit 1: a bounded wait inside the
+ * split-precision kernel gave up (the kernel returned early and u is
+ * incomplete).  The flags accumulate over calls until read.  The synchronous
+ * calls (dgsks, dgsks_status, dgsks_rhs, sgsks) keep their own flags and
+ * return GSKS_ERR_TIMEOUT instead.  Returns -1 if the flags could not be
+ * read. */
 int gsks_device_errors(void);
 
 /* ---- calibration -------------------------------------------------------- */
@@ -163,17 +174,19 @@ int gsks_device_errors(void);
 int gsks_probe_peak(int what, double *ops_per_s);
 
 /* ---- diagnostics -------------------------------------------------------- */
-/* Test hook of the split-precision form (no counterpart in the reference):
- * runs one device-resident evaluation like gsks_dgsks_device with
- * GSKS_SPLIT_BF16X3 and writes, for the first tile of the first CTA, the raw
- * tensor-core accumulators and the epilogue values of every (row, column) to
- * `dump` (128*128*5 floats: H, L, K, t, lo) and the call's scales to
- * `params_out` (alpha, sigma, 1/sigma, q as doubles at byte 0, the centre
- * (k doubles) at byte 64).  Device pointers. */
-int gsks_split_debug_dump(ks_t *kernel, int m, int n, int k, double *u, const int *umap,
-                          const double *XA, const int *amap, const double *XB, const int *bmap,
-                          const double *w, const int *wmap, float *dump, void *params_out,
-                          void *stream);
+/* Test hook of the split-precision form (no counterpart in the reference).
+ * Sets, for the calling thread's later split-precision calls (dgsks,
+ * dgsks_status, gsks_dgsks_device, dgsks_list, ...), the limit of the
+ * kernel's bounded waits in clock cycles (wait_cycles <= 0: the library's
+ * limit, about 2 s) and, with stall != 0, makes the bulk-copy role of every
+ * CTA issue nothing.  The tensor-core and epilogue roles then wait for data
+ * that never comes: each CTA's waits run out, it records the timeout, frees
+ * its tensor memory and returns.  Synchronous calls return GSKS_ERR_TIMEOUT
+ * (host u untouched); asynchronous ones set bit 1 of gsks_device_errors()
+ * and leave u incomplete.  This exercises the failure path of the bounded
+ * waits without faulting or hanging the GPU.  gsks_split_test_wait(0, 0)
+ * restores normal operation. */
+int gsks_split_test_wait(long long wait_cycles, int stall);
 
 /* ---- batched evaluation ------------------------------------------------ */
 /* dgsks_list: ntask independent kernel summations accumulated into one u.

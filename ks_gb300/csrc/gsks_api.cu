@@ -86,7 +86,7 @@ Ctx::~Ctx()
 {
   // Runs at host-thread exit; the CUDA runtime may already be gone at
   // process teardown, in which case the frees fail harmlessly.
-  for (DevBuf *b : {&partial, &err, &dA, &dA2, &dB, &dB2, &dw, &du, &dhi, &dhj, &dwork})
+  for (DevBuf *b : {&partial, &err, &dA, &dA2, &dB, &dB2, &dw, &du, &dhi, &dhj, &dwork, &rmaps, &serr})
     b->release();
   for (PinBuf *b : {&hA, &hA2, &hB, &hB2, &hw, &hu, &hhi, &hhj}) b->release();
   if (stream) cudaStreamDestroy(stream);
@@ -270,6 +270,25 @@ int unstage_host(Ctx *c, int m, double *u, const int *umap, int nrhs)
   return GSKS_OK;
 }
 
+SyncErrScope::SyncErrScope(Ctx *ctx) : c(ctx)
+{
+  ok = c->serr.ensure(2 * sizeof(int)) &&
+       cudaMemsetAsync(c->serr.p, 0, 2 * sizeof(int), c->stream) == cudaSuccess;
+  if (ok) c->cur_err = (int *)c->serr.p;
+}
+
+int SyncErrScope::finish()
+{
+  if (!ok) return GSKS_ERR_ALLOC;
+  int flags = 0;
+  cudaError_t e = cudaMemcpyAsync(&flags, c->serr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_status(e, "device error flags");
+  if (flags & DEVERR_TIMEOUT) return GSKS_ERR_TIMEOUT;
+  if (flags & DEVERR_MAP_RANGE) return GSKS_ERR_MAP_RANGE;
+  return GSKS_OK;
+}
+
 int read_device_errors(Ctx *c)
 {
   int flags = 0;
@@ -332,7 +351,7 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
   a.kp.coinc = coincidence_eps(k);
   a.nxa = nxa; a.nxb = nxb;
   a.partial = partial;
-  a.err = (int *)c->err.p;
+  a.err = err_word(c);
   a.nrhs = std::max(nrhs, 1);
   int launches = fp64_launch(a, p, u, umap, s);
   if (launches < 0) return GSKS_ERR_KERNEL_TYPE;
@@ -413,6 +432,7 @@ const char *gsks_error_string(int code)
     case GSKS_ERR_PRECISION: return "unsupported precision";
     case GSKS_ERR_NO_DEVICE: return "no CUDA device";
     case GSKS_ERR_TOO_LARGE: return "size exceeds the supported maximum";
+    case GSKS_ERR_TIMEOUT: return "a bounded wait in a kernel gave up; the result is incomplete";
     default: return "unknown status";
   }
 }
@@ -454,14 +474,13 @@ int dgsks_status(ks_t *kernel, int m, int n, int k,
   Ctx *c = get_ctx();
   if (!c) return tl_status;
   const int prec = effective_precision();
+  SyncErrScope se(c);
 
   if (is_device_pointer(XA)) {
     st = enqueue_fused(c, kernel, m, n, k, u, umap, XA, XA2, amap, -1, XB, XB2, bmap, -1,
                        w, wmap, kernel->hi, kernel->hj, prec, c->stream, false);
     if (st) return set_status(st, "dgsks");
-    cudaError_t e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return cuda_status(e, "dgsks");
-    return set_status(GSKS_OK, nullptr);
+    return set_status(se.finish(), "dgsks");
   }
 
   Staged v;
@@ -470,6 +489,8 @@ int dgsks_status(ks_t *kernel, int m, int n, int k,
   st = enqueue_fused(c, kernel, m, n, k, v.u, nullptr, v.A, v.A2, nullptr, m, v.B, v.B2,
                      nullptr, n, v.w, nullptr, v.hi, v.hj, prec, c->stream, false);
   if (st) return set_status(st, "dgsks");
+  // the flags first: a timed-out evaluation leaves u untouched
+  if ((st = se.finish()) != GSKS_OK) return set_status(st, "dgsks");
   st = unstage_host(c, m, u, umap);
   return set_status(st, "dgsks");
 }
@@ -542,13 +563,12 @@ int dgsks_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
   Ctx *c = get_ctx();
   if (!c) return tl_status;
   const int prec = effective_precision();
+  SyncErrScope se(c);
   if (is_device_pointer(XA)) {
     st = enqueue_rhs(c, kernel, m, n, k, nrhs, u, umap, XA, XA2, amap, -1, XB, XB2, bmap, -1, w, wmap,
                      kernel->hi, kernel->hj, prec, c->stream, false);
     if (st) return set_status(st, "dgsks_rhs");
-    const cudaError_t e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return cuda_status(e, "dgsks_rhs");
-    return set_status(GSKS_OK, nullptr);
+    return set_status(se.finish(), "dgsks_rhs");
   }
   Staged v;
   st = stage_host(c, kernel, m, n, k, u, umap, XA, XA2, amap, XB, XB2, bmap, w, wmap, v, nrhs);
@@ -556,6 +576,7 @@ int dgsks_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
   st = enqueue_rhs(c, kernel, m, n, k, nrhs, v.u, nullptr, v.A, v.A2, nullptr, m, v.B, v.B2, nullptr, n, v.w,
                    nullptr, v.hi, v.hj, prec, c->stream, false);
   if (st) return set_status(st, "dgsks_rhs");
+  if ((st = se.finish()) != GSKS_OK) return set_status(st, "dgsks_rhs");
   st = unstage_host(c, m, u, umap, nrhs);
   return set_status(st, "dgsks_rhs");
 }

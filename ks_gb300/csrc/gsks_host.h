@@ -30,8 +30,27 @@ struct Ctx {
   DevBuf partial, err;
   DevBuf dA, dA2, dB, dB2, dw, du, dhi, dhj, dwork;
   DevBuf rmaps;                // per-rhs u and w maps of the multi-rhs calls
+  DevBuf serr;                 // synchronous calls: [0] device error flags, [1] sgsks map-check flag
+  int *cur_err = nullptr;      // the error word kernels write (nullptr: err, the asynchronous calls')
   PinBuf hA, hA2, hB, hB2, hw, hu, hhi, hhj;
   ~Ctx();
+};
+
+// Device error word the kernels of the current call write.
+inline int *err_word(Ctx *c) { return c->cur_err ? c->cur_err : (int *)c->err.p; }
+
+// A synchronous call's own device error word: cleared on entry (stream
+// ordered), made current for the call's kernels, read by finish() after the
+// call's work is enqueued.  The asynchronous calls' flags in Ctx::err stay
+// as they were.
+struct SyncErrScope {
+  Ctx *c;
+  bool ok = false;
+  explicit SyncErrScope(Ctx *ctx);
+  ~SyncErrScope() { c->cur_err = nullptr; }
+  // Waits for the stream; GSKS_ERR_TIMEOUT if a bounded wait gave up,
+  // GSKS_ERR_MAP_RANGE for a map index out of range, else GSKS_OK.
+  int finish();
 };
 
 // Packed, identity-mapped device copy of a host-pointer call.
@@ -90,6 +109,10 @@ struct SplitListPlan {
   // (the partial layout), rescue list and its count
   size_t o_tg = 0, o_aoff = 0, o_pskip = 0, o_rl = 0, o_rc = 0;
   size_t o_ni = 0;   // work counter of the tile kernel
+  // polynomial tasks summed around row anchors: per-task source means and
+  // weight sums, the rows' v0^p
+  bool any_anch = false;
+  size_t o_ybar = 0, o_wsum = 0, o_rowc = 0;
 };
 int split_list_plan(SplitListPlan &P, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
                     const long long *pbase, int chunk, int nxa, int nxb, bool same_pool, cudaStream_t s);

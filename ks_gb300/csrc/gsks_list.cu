@@ -406,17 +406,18 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
   }
   st = list_plan_run(B.plan, c, du, dXA, dXA2, dXB, dXB2, dw, s, &launches);
   if (st) return set_status(st, "dgsks_list");
-  cudaError_t e = cudaSuccess;
-  if (!dev) {
-    e = cudaMemcpyAsync(u, du, (size_t)nu * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) return cuda_status(e, "dgsks_list copy back");
-  }
+  // the flags first: host arrays keep their u when the evaluation failed
   int flags = 0;
-  cudaMemcpyAsync(&flags, B.plan.err.p, sizeof(int), cudaMemcpyDeviceToHost, s);
-  e = cudaStreamSynchronize(s);
+  cudaError_t e = cudaMemcpyAsync(&flags, B.plan.err.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_status(e, "dgsks_list");
   if (flags & DEVERR_MAP_RANGE) return set_status(GSKS_ERR_MAP_RANGE, "dgsks_list");
-  if (flags & DEVERR_TIMEOUT) return set_status(GSKS_ERR_CUDA, "dgsks_list: a bounded wait gave up");
+  if (flags & DEVERR_TIMEOUT) return set_status(GSKS_ERR_TIMEOUT, "dgsks_list");
+  if (!dev) {
+    e = cudaMemcpyAsync(u, du, (size_t)nu * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "dgsks_list copy back");
+  }
   note_launches(launches);
   return set_status(GSKS_OK, nullptr);
 }

@@ -78,8 +78,7 @@ int sgsks_status(ks_t *kernel, int m, int n, int k,
   const bool varbw = kernel->type == KS_GAUSSIAN_VAR_BANDWIDTH;
   const size_t mk = (size_t)m * k, nk = (size_t)n * k;
   bool ok = c->dA.ensure(mk * 8) && c->dB.ensure(nk * 8) && c->dA2.ensure((size_t)m * 8) &&
-            c->dB2.ensure((size_t)n * 8) && c->du.ensure((size_t)m * 8) && c->dw.ensure((size_t)n * 8) &&
-            c->rmaps.ensure(sizeof(int));
+            c->dB2.ensure((size_t)n * 8) && c->du.ensure((size_t)m * 8) && c->dw.ensure((size_t)n * 8);
   if (ok && varbw) ok = c->dhi.ensure((size_t)m * 8) && c->dhj.ensure((size_t)n * 8);
   if (!ok) return set_status(GSKS_ERR_ALLOC, "sgsks");
   double *dA = (double *)c->dA.p, *dB = (double *)c->dB.p, *dA2 = (double *)c->dA2.p, *dB2 = (double *)c->dB2.p;
@@ -87,10 +86,12 @@ int sgsks_status(ks_t *kernel, int m, int n, int k,
   double *dhi = varbw ? (double *)c->dhi.p : nullptr, *dhj = varbw ? (double *)c->dhj.p : nullptr;
   cudaStream_t s = c->stream;
   const int prec = effective_precision();
+  SyncErrScope se(c);   // clears both words of the synchronous calls' flags
+  if (!se.ok) return set_status(GSKS_ERR_ALLOC, "sgsks");
 
   if (is_device_pointer(XA)) {
-    int *bad = (int *)c->rmaps.p;   // its own flag: the context's error word keeps earlier calls' flags
-    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), s);
+    int *bad = (int *)c->serr.p + 1;   // the gather's map-check flag
+    cudaError_t e = cudaSuccess;
     const int blocks = std::max(1, std::min(1024, (std::max(m, n) + 7) / 8));
     gather_rows_f32<<<blocks, 256, 0, s>>>(m, k, XA, amap, varbw ? kernel->hi : nullptr, u, umap, dA, dA2, dhi, du,
                                            bad);
@@ -105,6 +106,7 @@ int sgsks_status(ks_t *kernel, int m, int n, int k,
     st = enqueue_fused(c, kernel, m, n, k, du, nullptr, dA, dA2, nullptr, m, dB, dB2, nullptr, n, dw, nullptr, dhi,
                        dhj, prec, s, false);
     if (st) return set_status(st, "sgsks");
+    if ((st = se.finish()) != GSKS_OK) return set_status(st, "sgsks");   // a timed-out evaluation leaves u as it was
     scatter_u_f32<<<(m + 255) / 256, 256, 0, s>>>(m, du, umap, u);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -160,6 +162,7 @@ int sgsks_status(ks_t *kernel, int m, int n, int k,
   st = enqueue_fused(c, kernel, m, n, k, du, nullptr, dA, dA2, nullptr, m, dB, dB2, nullptr, n, dw, nullptr, dhi,
                      dhj, prec, s, false);
   if (st) return set_status(st, "sgsks");
+  if ((st = se.finish()) != GSKS_OK) return set_status(st, "sgsks");
   e = cudaMemcpyAsync(c->hu.p, du, (size_t)m * 8, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_status(e, "sgsks");

@@ -127,6 +127,14 @@ struct Params {          // per call, computed on the device
   // tasks); each task's scale follows from them (task_params_kernel).
   double mx_c, sq_c, mx_u, sq_u;
   int k;
+  // Polynomial kernels of integer power 1..4 (anch): each target row carries
+  // an anchor v0 near its values v = cons + scal x.y; the epilogue sums
+  // K - v0^p in FP32 and the reduction adds v0^p times the sum of the
+  // weights in FP64.  sg = scal * g / 2 maps accumulator units to v.
+  int anch;
+  float sg;
+  int pw;                // anch: the power
+  double pscal, pcons;   // anch: the kernel's scal and cons
 };
 
 // Kernel selector of the batched (list) form: the epilogue dispatches on each
@@ -149,7 +157,9 @@ struct __align__(16) TaskParam {
   // grid q (list form; Gaussian tasks are scaled by their bandwidth)
   double sc, sig2, g, q;
   int gfast;             // Gaussian without flags: low norm parts folded (as Params::gfast)
-  int pad[3];
+  int anch;              // polynomial of power 1..4 summed around row anchors (as Params::anch)
+  float sg;              // scal * g / 2 (anch)
+  int pad;
 };
 static_assert(sizeof(TaskParam) % 16 == 0, "TaskParam is copied by the bulk-copy engine");
 
@@ -319,7 +329,7 @@ __device__ LapParam lap_param(double scal, double powe)
 // kt = KS_LIST: the list form, whose tasks mix centred (distance) and
 // uncentred (inner-product) kernels: the centre is the box's, the scale covers
 // the uncentred coordinates too, and the thresholds are set per task later.
-__global__ void params_kernel(int k, int kt, double scal, double powe, float tau, const long long *bbox,
+__global__ void params_kernel(int k, int kt, double scal, double cons, double powe, float tau, const long long *bbox,
                               double *centre, Params *P)
 {
   __shared__ double s_sq[1024], s_mx[1024], s_sqc[1024], s_mxc[1024];
@@ -400,6 +410,11 @@ __global__ void params_kernel(int k, int kt, double scal, double powe, float tau
     P->exact_t1 = (q <= 2.0 * sigma * sigma * 0x1p-14) ? 1 : 0;
     P->gfast = (kt == KS_GAUSSIAN && P->exact_t1 && !P->any_flag) ? 1 : 0;
     P->ff_ok = (s_mx[0] <= 0x1p50) ? 1 : 0;
+    P->anch = (kt == KS_POLYNOMIAL && powe == rint(powe) && powe >= 1.0 && powe <= 4.0) ? 1 : 0;
+    P->sg = (float)(scal * 0.5 * P->g);
+    P->pw = (int)powe;
+    P->pscal = scal;
+    P->pcons = cons;
   }
 
 }
@@ -438,7 +453,9 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   T.rc = (float)(-g);
   T.exact = (q <= g) ? 1 : 0;
   T.gfast = 0;
-  T.pad[0] = T.pad[1] = T.pad[2] = 0;
+  T.anch = (kp.type == KS_POLYNOMIAL && kp.pmode == POW_INT && kp.pint >= 1 && kp.pint <= 4) ? 1 : 0;
+  T.sg = (float)(kp.scal * 0.5 * g);
+  T.pad = 0;
   if (kp.type == KS_GAUSSIAN) {
     T.s2 = (float)s2;                      // the rechecks work from the pool coordinates
     T.s2l = (float)(s2 - (double)T.s2);
@@ -471,6 +488,79 @@ __global__ void pool_split(long long n, const double *__restrict__ X, float2 *__
   }
 }
 
+// Sums over the sources j0 .. j1-1 of every coordinate (ysum[p] = inv_n times
+// the sum, p < k) and of the weights (*wsum), in FP64 and in a fixed order:
+// the block's threads take the k + 1 columns in passes, each column split
+// over equal strided groups of sources, the groups then added in order.
+// sh: blockDim.x doubles of shared memory.
+__device__ void block_source_sums(int j0, int j1, int k, const double *__restrict__ X,
+                                  const int *__restrict__ map, int npool, int *err,
+                                  const double *__restrict__ w, const int *__restrict__ wmap, double inv_n,
+                                  double *ysum, double *wsum, double *sh)
+{
+  const int kk = k + 1, t = threadIdx.x;
+  for (int p0 = 0; p0 < kk; p0 += blockDim.x) {
+    const int cols = min((int)blockDim.x, kk - p0);
+    const int sub = blockDim.x / cols;           // threads per column
+    const int c = t % cols, grp = t / cols;
+    double s = 0.0;
+    if (grp < sub) {
+      const int p = p0 + c;
+      for (int j = j0 + grp; j < j1; j += sub)
+        s += p < k ? X[(size_t)pool_index(map, j, npool, err) * k + p] : w[wmap ? wmap[j] : j];
+    }
+    sh[t] = s;
+    __syncthreads();
+    if (t < cols) {
+      double r = 0.0;
+      for (int q = 0; q < sub; q++) r += sh[q * cols + t];
+      if (p0 + t < k) ysum[p0 + t] = r * inv_n;
+      else *wsum = r;
+    }
+    __syncthreads();
+  }
+}
+
+// Anchor point of a single call's polynomial kernel: the mean of the gathered
+// sources, and the sum of their weights.  Pass 1: block b sums its range of
+// sources into part[b * (k + 1) ..]; pass 2 (one block) adds the blocks in order.
+__global__ void anchor_partial(int n, int k, const double *__restrict__ XB, const int *__restrict__ bmap, int nxb,
+                               const double *__restrict__ w, const int *__restrict__ wmap, int *err,
+                               double *__restrict__ part)
+{
+  extern __shared__ double sh_sum[];
+  const int per = (n + gridDim.x - 1) / gridDim.x;
+  const int j0 = min(n, blockIdx.x * per), j1 = min(n, j0 + per);
+  double *out = part + (size_t)blockIdx.x * (k + 1);
+  block_source_sums(j0, j1, k, XB, bmap, nxb, err, w, wmap, 1.0, out, out + k, sh_sum);
+}
+
+__global__ void anchor_final(int nblk, int n, int k, const double *__restrict__ part, double *__restrict__ ybar,
+                             double *__restrict__ wsum)
+{
+  for (int p = threadIdx.x; p <= k; p += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; b++) s += part[(size_t)b * (k + 1) + p];
+    if (p < k) ybar[p] = s / (double)n;
+    else *wsum = s;
+  }
+}
+
+// The same per task of the list form (one block per task; tasks that are not
+// anchored, or empty, are skipped): ybar[t * k ..] and wsum[t].
+__global__ void list_anchor(int ntask, int k, const TaskParam *__restrict__ tp, const SplitTaskGeo *__restrict__ tg,
+                            const double *__restrict__ XB, const int *__restrict__ b_idx, int nxb,
+                            const double *__restrict__ w, const int *__restrict__ w_idx, int *err,
+                            double *__restrict__ ybar, double *__restrict__ wsum)
+{
+  extern __shared__ double sh_sum[];
+  const int t = blockIdx.x;
+  if (t >= ntask || !tp[t].anch || tg[t].n <= 0 || tg[t].m <= 0) return;
+  const SplitTaskGeo G = tg[t];
+  block_source_sums(G.b0, G.b0 + G.n, k, XB, b_idx, nxb, err, w, w_idx, 1.0 / (double)G.n,
+                    ybar + (size_t)t * k, wsum + t, sh_sum);
+}
+
 // Tile images: per tile, NBLK slice blocks in the no-swizzle K-major core-matrix
 // layout (element (r, p) at (p/8)*rows*16 + r*16 + (p%8)*2 bytes), then the
 // point metadata.  One thread per point.
@@ -481,7 +571,8 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
                             const int *__restrict__ wmap, const double *__restrict__ hvec, int kt,
                             const double *__restrict__ centre, const Params *__restrict__ P,
                             uint8_t *__restrict__ img, const int2 *__restrict__ tiles,
-                            const int *__restrict__ tile_task, const TaskParam *__restrict__ tp)
+                            const int *__restrict__ tile_task, const TaskParam *__restrict__ tp,
+                            const double *__restrict__ ybar, double *__restrict__ rowc)
 {
   const int tile = blockIdx.x, r = threadIdx.x;
   int pt = tile * BM + r;
@@ -573,6 +664,35 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
     mt.h = (float)hv;
     mt.pad[1] = __float_as_int((float)(hv - (double)mt.h));
   }
+  const bool anch = side == 0 && (TT ? TT->anch != 0 : P->anch != 0);
+  if (anch) {
+    // Polynomial rows summed around an anchor: H0 = x.ybar in accumulator
+    // units (x.y = (g/2)(H + L)), rounded to an integer so that H - H0 is
+    // exact, and v0 = cons + scal (g/2) H0; the row keeps H0 (n_hi) and the
+    // binomial coefficients c_i = C(p, i) v0^(p-i), i = 1..p-1 (n_lo, w, h);
+    // rowc gets v0^p in FP64.  Padding rows: all zero.
+    mt.n_hi = mt.n_lo = mt.w = mt.h = 0.0f;
+    if (valid) {
+      const double *yb = ybar + (TT ? (size_t)tile_task[tile] * k : 0);
+      double A = 0.0;
+      for (int p = 0; p < k; p++) A = fma(x[p], yb[p], A);
+      const double G = 0.5 * g;
+      const double H0 = fmin(fmax(rint(A / G), -0x1p24), 0x1p24);
+      const double scal = TT ? TT->kp.scal : P->pscal, cons = TT ? TT->kp.cons : P->pcons;
+      const int pw = TT ? TT->kp.pint : P->pw;
+      const double v0 = fma(scal * G, H0, cons);
+      const double v2 = v0 * v0;
+      double c1 = 1.0, c2 = 0.0, c3 = 0.0, vp = v0;
+      if (pw == 2) { c1 = 2.0 * v0; vp = v2; }
+      else if (pw == 3) { c1 = 3.0 * v2; c2 = 3.0 * v0; vp = v2 * v0; }
+      else if (pw == 4) { c1 = 4.0 * v2 * v0; c2 = 6.0 * v2; c3 = 4.0 * v0; vp = v2 * v2; }
+      mt.n_hi = (float)H0;
+      mt.n_lo = (float)c1;
+      mt.w = (float)c2;
+      mt.h = (float)c3;
+      rowc[pt] = vp;
+    }
+  }
   if (side == 0) {
     ((PtMeta *)(base + NBLK * bb))[r] = mt;
     return;
@@ -607,7 +727,8 @@ struct TileArgs {
   float *pskip;                     // W sums of the groups left to the row rescue (the partial layout)
   int ldp;
   int *err;
-  float *dump;                      // test hook: H, L, t, lo, K of CTA 0's first tile
+  long long wait_limit;             // clock cycles before a wait gives up
+  int stall;                        // test hook: the producer issues nothing (the waits run out)
   // list form: explicit work items and per-task parameters (nullptr otherwise)
   const SplitItem *tab;
   int ntab;
@@ -645,6 +766,7 @@ struct SplitSmem {
   uint64_t b_full[NSTAGE], b_empty[NSTAGE];
   uint64_t m_full[NMETA], m_empty[NMETA];
   uint64_t t_full[2], t_empty[2];
+  uint64_t r_full[2], r_empty[2];       // row-sum exchange of the epilogue groups, by item parity
   uint64_t drain;
   uint32_t tmem_base;
   int abort;
@@ -1261,27 +1383,41 @@ __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint
   acc[0] = lo2(A[0]); acc[1] = hi2(A[0]); acc[2] = lo2(A[1]); acc[3] = hi2(A[1]);
 }
 
-// Test hook: raw accumulators and epilogue values of NC columns from c0.
-template <int KT, int NC>
-__device__ void dump_chunk(float *dump, int row, int c0, const uint32_t (&h)[NC], const uint32_t (&l)[NC],
-                           const SrcMeta *bm, const PtMeta &am, float rc, const KParams &kp)
+// NC columns of one row, polynomial of integer power PW in 1..4, summed
+// around the row's anchor v0: v = v0 + d with d = sg ((H - H0) + L) (H - H0
+// exact: both are integers below 2^24), and
+//   K - v0^PW = d (c1 + d (c2 + d (c3 + d)))   (binomial expansion, Horner
+// form, c_i = C(PW, i) v0^(PW-i) from the row's metadata).  The reduction adds
+// v0^PW times the sum of all weights in FP64, so the FP32 sums carry only the
+// variation of K around v0^PW: where K sits on a large constant (v near cons,
+// the sum of K w cancelling), FP32 rounding of K itself would otherwise
+// dominate the error.  Padding columns: finite values, weight 0.
+template <int NC, int PW>
+__device__ __forceinline__ void epi_chunk_anchor(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
+                                                 const SrcMeta *__restrict__ bm, int c0, const PtMeta &am, float sg,
+                                                 float (&acc)[4])
 {
-  for (int j = 0; j < NC; j++) {
-    const int c = c0 + j;
-    float *dp = dump + ((size_t)row * BN + c) * 5;
-    const float H = __uint_as_float(h[j]), L = __uint_as_float(l[j]);
-    dp[0] = H; dp[1] = L;
-    if constexpr (kt_uses_norms(KT)) {
-      float t, lo, s;
-      assemble<false>(H, L, am.n_hi, am.n_lo, bm->n_hi[c], bm->n_lo[c], rc, t, lo, s);
-      dp[2] = 0.f;
-      if constexpr (KT != KS_LAPLACE) dp[2] = kval32<KT>(t, lo, 0.f, am.h, bm->h[c], kp);
-      dp[3] = t; dp[4] = lo;
-    } else {
-      dp[2] = kval32<KT>(0.f, 0.f, fmaf(L, rc, H * rc) * -0.5f, 0.f, 0.f, kp);
-      dp[3] = dp[4] = 0.f;
+  const uint64_t H0 = pk2(am.n_hi, am.n_hi), SG = pk2(sg, sg);
+  const uint64_t C1 = pk2(am.n_lo, am.n_lo), C2 = pk2(am.w, am.w), C3 = pk2(am.h, am.h);
+  uint64_t A[2] = {pk2(acc[0], acc[1]), pk2(acc[2], acc[3])};
+#pragma unroll
+  for (int j4 = 0; j4 < NC; j4 += 4) {
+    const float4 ww = ld4(&bm->w[c0 + j4]);
+#pragma unroll
+    for (int p2 = 0; p2 < 2; p2++) {
+      const int j = j4 + 2 * p2;
+      const uint64_t H = pk2(__uint_as_float(h[j]), __uint_as_float(h[j + 1]));
+      const uint64_t L = pk2(__uint_as_float(l[j]), __uint_as_float(l[j + 1]));
+      const uint64_t D = mul2(add2(sub2(H, H0), L), SG);
+      uint64_t R;
+      if constexpr (PW == 1) R = D;
+      else if constexpr (PW == 2) R = mul2(D, add2(D, C1));
+      else if constexpr (PW == 3) R = mul2(D, fma2(D, add2(D, C2), C1));
+      else R = mul2(D, fma2(D, fma2(D, add2(D, C3), C2), C1));
+      A[p2] = fma2(R, pk2(f4(ww, 2 * p2), f4(ww, 2 * p2 + 1)), A[p2]);
     }
   }
+  acc[0] = lo2(A[0]); acc[1] = hi2(A[0]); acc[2] = lo2(A[1]); acc[3] = hi2(A[1]);
 }
 
 // Kernels whose FP32 values may fall below the FP32 range while FP64 keeps
@@ -1300,7 +1436,7 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 template <int KT, bool LISTED = false>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
                                               const SrcMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
-                                              bool gfast, bool dump, const LTab &ltab, double &racc,
+                                              bool gfast, const LTab &ltab, double &racc,
                                               float &bsk, float *wq)
 {
   // Gaussian kinds with the pools' float-pair copies: flagged pairs are
@@ -1325,7 +1461,6 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     tmem_ld<NCH>(tH + c0, h);
     tmem_ld<NCH>(tH + 128 + c0, l);
     tmem_ld_wait();
-    if (dump) dump_chunk<KT, NCH>(a.dump, row, c0, h, l, bm, am, rc, T.kp);
     if constexpr (KT == KS_GAUSSIAN) {
       if (gfast) { epi_chunk_gfast<NCH>(h, l, bm, c0, am.n_hi, rc, acc); continue; }
     }
@@ -1359,7 +1494,13 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
       }
     } else if constexpr (KT == KS_POLYNOMIAL) {
       const int pw = T.kp.pmode == POW_INT ? T.kp.pint : 0;
-      if (pw == 2) epi_chunk_ip<KT, NCH, 2>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      if (T.anch) {
+        if (pw == 3) epi_chunk_anchor<NCH, 3>(h, l, bm, c0, am, T.sg, acc);
+        else if (pw == 2) epi_chunk_anchor<NCH, 2>(h, l, bm, c0, am, T.sg, acc);
+        else if (pw == 4) epi_chunk_anchor<NCH, 4>(h, l, bm, c0, am, T.sg, acc);
+        else epi_chunk_anchor<NCH, 1>(h, l, bm, c0, am, T.sg, acc);
+      }
+      else if (pw == 2) epi_chunk_ip<KT, NCH, 2>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
       else if (pw == 3) epi_chunk_ip<KT, NCH, 3>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
       else if (pw == 4) epi_chunk_ip<KT, NCH, 4>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
       else if (pw == 1) epi_chunk_ip<KT, NCH, 1>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
@@ -1422,6 +1563,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     for (int s = 0; s < NSTAGE; s++) { mbar_init(&S->b_full[s], 1); mbar_init(&S->b_empty[s], 1); }
     for (int s = 0; s < NMETA; s++) { mbar_init(&S->m_full[s], 1); mbar_init(&S->m_empty[s], EPI_WARPS); }
     for (int b = 0; b < 2; b++) { mbar_init(&S->t_full[b], 1); mbar_init(&S->t_empty[b], EPI_WARPS); }
+    for (int b = 0; b < 2; b++) {   // one arrive per thread: groups 1.. fill, group 0 empties
+      mbar_init(&S->r_full[b], 32 * 4 * (EPI_GROUPS - 1));
+      mbar_init(&S->r_empty[b], 32 * 4);
+    }
     mbar_init(&S->drain, 1);
     S->abort = 0;
     S->never = 0;
@@ -1441,7 +1586,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     // Resident (k <= KPAD_MAX): the target tile image once per item, the source
     // operands once per tile.  Streaming: the target metadata once per item,
     // then per tile and k-chunk one stage holding both operands' chunk.
-    if (lane == 0) {
+    if (lane == 0 && !a.stall) {
       int g = 0, tt = 0;
       int a_issued = -1;                  // item index of the last target copy
       int b_last[NSTAGE], m_last[NMETA];  // use count of the last copy per stage / meta slot
@@ -1453,7 +1598,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       // (written before the arrive on a_full, which releases it).
       int item = blockIdx.x;
       for (int it = 0; !*abort && !stop; it++) {
-        if (it > 0 && !mbar_wait(&S->a_empty, (it - 1) & 1, abort, WAIT_LIMIT)) break;
+        if (it > 0 && !mbar_wait(&S->a_empty, (it - 1) & 1, abort, a.wait_limit)) break;
         if (item >= items) {
           S->islot[it & 1] = -1;
           mbar_arrive(&S->a_full);
@@ -1479,7 +1624,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           const uint8_t *imgB = a.imgB + (size_t)tj * b_bytes;
           for (int c = 0; c < L.nch; c++, g++) {
             const int st = g % L.nstage, u = g / L.nstage;
-            if (u > 0 && !mbar_wait(&S->b_empty[st], (u - 1) & 1, abort, WAIT_LIMIT)) { stop = true; break; }
+            if (u > 0 && !mbar_wait(&S->b_empty[st], (u - 1) & 1, abort, a.wait_limit)) { stop = true; break; }
             uint8_t *dst = sStage + st * L.stage_bytes;
             if (resident) {
               mbar_arrive_expect_tx(&S->b_full[st], (uint32_t)L.chunk_op);
@@ -1493,7 +1638,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           }
           if (stop) break;
           const int ms = tt % NMETA, mu = tt / NMETA;
-          if (mu > 0 && !mbar_wait(&S->m_empty[ms], (mu - 1) & 1, abort, WAIT_LIMIT)) break;
+          if (mu > 0 && !mbar_wait(&S->m_empty[ms], (mu - 1) & 1, abort, a.wait_limit)) break;
           mbar_arrive_expect_tx(&S->m_full[ms], (uint32_t)meta_bytes);
           bulk_g2s(sBm + ms * meta_bytes, imgB + a_op, (uint32_t)meta_bytes, &S->m_full[ms]);
           m_last[ms] = mu;
@@ -1520,17 +1665,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       int g = 0, tc = 0;
       bool stop = false;
       for (int it = 0; !*abort && !stop; it++) {
-        if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
+        if (!mbar_wait(&S->a_full, it & 1, abort, a.wait_limit)) break;
         const int item = ((volatile int *)S->islot)[it & 1];
         if (item < 0) break;
         const ItemGeo G = item_geo(a, item);
         for (int tj = G.t0; tj < G.t1 && !stop; tj++, tc++) {
           const int buf = tc & 1;
-          if (tc >= 2 && !mbar_wait(&S->t_empty[buf], ((tc >> 1) - 1) & 1, abort, WAIT_LIMIT)) { stop = true; break; }
+          if (tc >= 2 && !mbar_wait(&S->t_empty[buf], ((tc >> 1) - 1) & 1, abort, a.wait_limit)) { stop = true; break; }
           const uint32_t dH = tmem + buf * 256, dL = tmem + buf * 256 + 128;
           for (int c = 0; c < L.nch; c++, g++) {
             const int st = g % L.nstage;
-            if (!mbar_wait(&S->b_full[st], (g / L.nstage) & 1, abort, WAIT_LIMIT)) { stop = true; break; }
+            if (!mbar_wait(&S->b_full[st], (g / L.nstage) & 1, abort, a.wait_limit)) { stop = true; break; }
             tc_fence_after();
             const uint32_t sbase = smem_addr(sStage + st * L.stage_bytes);
             const uint32_t a0 = resident ? smem_addr(sA) : sbase;
@@ -1576,10 +1721,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       T0.kp = a.kp; T0.t_flag = P->t_flag; T0.rho = P->rho;
       T0.s2 = (float)s2; T0.s2l = (float)(s2 - (double)T0.s2);
       T0.lap = P->lap; T0.any_flag = P->any_flag; T0.centred = P->centred;
+      T0.anch = P->anch; T0.sg = P->sg;
     }
     int g = 0, tc = 0;
     for (int it = 0; !*abort; it++) {
-      if (!mbar_wait(&S->a_full, it & 1, abort, WAIT_LIMIT)) break;
+      if (!mbar_wait(&S->a_full, it & 1, abort, a.wait_limit)) break;
       const int item = ((volatile int *)S->islot)[it & 1];
       if (item < 0) break;
       const ItemGeo G = item_geo(a, item);
@@ -1592,49 +1738,57 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       bool ok = true;
       for (int tj = G.t0; tj < G.t1; tj++, g++, tc++) {
         const int ms = g % NMETA, buf = tc & 1;
-        if (!mbar_wait(&S->t_full[buf], (tc >> 1) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
-        if (!mbar_wait(&S->m_full[ms], (g / NMETA) & 1, abort, WAIT_LIMIT)) { ok = false; break; }
+        if (!mbar_wait(&S->t_full[buf], (tc >> 1) & 1, abort, a.wait_limit)) { ok = false; break; }
+        if (!mbar_wait(&S->m_full[ms], (g / NMETA) & 1, abort, a.wait_limit)) { ok = false; break; }
         tc_fence_after();
         const SrcMeta *bm = (const SrcMeta *)(sBm + ms * meta_bytes);
         const int ncols = a.tab ? a.btile_cols[tj] : min(BN, a.n - tj * BN);
         const uint32_t tH = tmem + ((uint32_t)(qd * 32) << 16) + buf * 256;
-        const bool dump = a.dump && blockIdx.x == 0 && tc == 0;
         if constexpr (KT == KS_LIST) {
           const float lrc = T.rc;              // the task's scale (centred or not)
           const bool lexact = T.exact != 0;
           switch (T.kp.type) {
             case KS_GAUSSIAN:   // scaled units, as a single call
-              tile_epilogue<KS_GAUSSIAN>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_GAUSSIAN>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, ltab, racc, bsk, wq); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_POLYNOMIAL:
-              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE, true>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_LAPLACE, true>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_TANH:
-              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_QUARTIC:
-              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_MULTIQUADRATIC:
-              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             default:
-              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, dump, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
           }
         } else {
-          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, dump, ltab, racc, bsk, wq);
+          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, ltab, racc, bsk, wq);
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) { mbar_arrive(&S->t_empty[buf]); mbar_arrive(&S->m_empty[ms]); }
       }
       if (!ok) break;
-      // combine the groups' row sums in group order (double-buffered by item parity)
-      double (*xs)[BM] = S->rsum[it & 1];
-      float (*xb)[BM] = S->rskip[it & 1];
-      if (grp > 0) { xs[grp - 1][row] = racc; xb[grp - 1][row] = bsk; }
-      asm volatile("bar.sync 1, %0;" ::"n"(32 * EPI_WARPS) : "memory");
-      if (grp == 0) {
+      // Combine the groups' row sums in group order, through a slot per item
+      // parity: groups 1.. write theirs and arrive on r_full, group 0 waits,
+      // reads and arrives on r_empty.  Every wait is bounded (a block-wide
+      // barrier here could wait forever for a warp whose earlier wait gave up).
+      const int rb = it & 1, ru = it >> 1;   // slot, and its earlier uses
+      double (*xs)[BM] = S->rsum[rb];
+      float (*xb)[BM] = S->rskip[rb];
+      if (grp > 0) {
+        if (ru > 0 && !mbar_wait(&S->r_empty[rb], (ru - 1) & 1, abort, a.wait_limit)) break;
+        xs[grp - 1][row] = racc;
+        xb[grp - 1][row] = bsk;
+        mbar_arrive(&S->r_full[rb]);
+      } else {
+        if (!mbar_wait(&S->r_full[rb], ru & 1, abort, a.wait_limit)) break;
         for (int q = 0; q < EPI_GROUPS - 1; q++) { racc += xs[q][row]; bsk += xb[q][row]; }
+        mbar_arrive(&S->r_empty[rb]);
         const bool rowf = KT == KS_LIST ? (T.kp.type == KS_GAUSSIAN && T.gfast != 0) : (KT == KS_GAUSSIAN && gfast);
         if (rowf) {                               // the row's low-norm factor
           racc *= (double)am.h;
@@ -1658,15 +1812,19 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
 // sums (pskip holds their sums of |w|, b): their part of row i is below
 // 2^-96 b.  Where that could reach 2^-27 of |s| (in practice: rows whose
 // every value is that small) the row goes to the rescue list instead.
+// Anchored polynomial rows (rowc != nullptr): the row's v0^p times the sum of
+// all weights, *wsum, is added in FP64.
 __global__ void split_reduce(int m, int nsc, int ldp, const double *__restrict__ partial,
                              const float *__restrict__ pskip, double *__restrict__ u, const int *__restrict__ umap,
-                             int *__restrict__ rlist, int *__restrict__ rcount)
+                             int *__restrict__ rlist, int *__restrict__ rcount, const double *__restrict__ rowc,
+                             const double *__restrict__ wsum)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   double s = 0.0;
   float b = 0.0f;
   for (int c = 0; c < nsc; c++) s += partial[(size_t)c * ldp + i];
+  if (rowc) s += rowc[i] * *wsum;
   if (pskip) {
     for (int c = 0; c < nsc; c++) b += pskip[(size_t)c * ldp + i];
     if (b > 0.0f && fabs(s) < 0x1p-69 * (double)b) {
@@ -1761,9 +1919,9 @@ size_t smem_bytes(int kpad, int kt)
 
 }  // namespace split
 
-// Test hook state (gsks_split_debug_dump): per host thread.
-thread_local float *tl_split_dump = nullptr;
-thread_local void *tl_split_params = nullptr;
+// Test hook state (gsks_split_test_wait): per host thread.
+thread_local long long tl_split_wait = 0;
+thread_local int tl_split_stall = 0;
 
 // ---------------------------------------------------------------------------
 int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const int *umap,
@@ -1820,7 +1978,14 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const size_t o_ni = o_rc + (defer ? al(4) : 0);   // work counter
   const size_t o_xaf = o_ni + al(4);
   const size_t o_xbf = o_xaf + (ff ? al((size_t)nxa * k * sizeof(float2)) : 0);
-  const size_t total = o_xbf + (ff && !same_pool ? al((size_t)nxb * k * sizeof(float2)) : 0);
+  // anchored polynomial: source mean and weight sum (ybar | wsum | block
+  // partials) and the rows' v0^p
+  const bool anch = ker->type == KS_POLYNOMIAL && ker->powe == rint(ker->powe) && ker->powe >= 1.0 &&
+                    ker->powe <= 4.0;
+  const int nab = std::max(1, std::min(sms, (n + 255) / 256));   // blocks of the first anchor pass
+  const size_t o_anc = o_xbf + (ff && !same_pool ? al((size_t)nxb * k * sizeof(float2)) : 0);
+  const size_t o_rowc = o_anc + (anch ? al(((size_t)k + 1 + (size_t)nab * (k + 1)) * 8) : 0);
+  const size_t total = o_rowc + (anch ? al((size_t)m * 8) : 0);
   uint8_t *ws = nullptr;
   if (stream_ordered_alloc) {
     cudaError_t e = cudaMallocAsync((void **)&ws, total, s);
@@ -1843,13 +2008,20 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
     const int blocks = (int)std::max<long long>((k + 255) / 256,
                                                 std::min<long long>(8LL * sms, std::max<long long>(1, (tot + 255) / 256)));
     bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(m, n, k, XA, amap, nxa, XB, bmap, nxb,
-                                                               (int *)c->err.p, bbox);
+                                                               err_word(c), bbox);
   }
-  params_kernel<<<1, 1024, 0, s>>>(k, ker->type, ker->scal, ker->powe, tau, bbox, centre, P);
-  pack_kernel<<<ntm, BM, 0, s>>>(0, m, k, kpad, XA, amap, nxa, (int *)c->err.p, nullptr, nullptr, hi, ker->type,
-                                 centre, P, ws + o_a, nullptr, nullptr, nullptr);
-  pack_kernel<<<ntn, BN, 0, s>>>(1, n, k, kpad, XB, bmap, nxb, (int *)c->err.p, w, wmap, hj, ker->type, centre,
-                                 P, ws + o_b, nullptr, nullptr, nullptr);
+  params_kernel<<<1, 1024, 0, s>>>(k, ker->type, ker->scal, ker->cons, ker->powe, tau, bbox, centre, P);
+  double *ybar = anch ? (double *)(ws + o_anc) : nullptr;
+  double *rowc = anch ? (double *)(ws + o_rowc) : nullptr;
+  if (anch) {
+    double *part = ybar + k + 1;
+    anchor_partial<<<nab, 256, 256 * sizeof(double), s>>>(n, k, XB, bmap, nxb, w, wmap, err_word(c), part);
+    anchor_final<<<1, 256, 0, s>>>(nab, n, k, part, ybar, ybar + k);
+  }
+  pack_kernel<<<ntm, BM, 0, s>>>(0, m, k, kpad, XA, amap, nxa, err_word(c), nullptr, nullptr, hi, ker->type,
+                                 centre, P, ws + o_a, nullptr, nullptr, nullptr, ybar, rowc);
+  pack_kernel<<<ntn, BN, 0, s>>>(1, n, k, kpad, XB, bmap, nxb, err_word(c), w, wmap, hj, ker->type, centre,
+                                 P, ws + o_b, nullptr, nullptr, nullptr, nullptr, nullptr);
 
   TileArgs a{};
   a.m = m; a.n = n; a.k = k; a.kpad = kpad; a.kt = ker->type;
@@ -1873,25 +2045,23 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   a.pskip = defer ? (float *)(ws + o_ps) : nullptr;
   a.next_item = (int *)(ws + o_ni);
   a.ldp = ldp;
-  a.err = (int *)c->err.p;
-  a.dump = tl_split_dump;
-  if (tl_split_params) {
-    cudaMemcpyAsync(tl_split_params, P, sizeof(Params), cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync((uint8_t *)tl_split_params + 64, centre, (size_t)k * 8, cudaMemcpyDeviceToDevice, s);
-  }
+  a.err = err_word(c);
+  a.wait_limit = tl_split_wait > 0 ? tl_split_wait : WAIT_LIMIT;
+  a.stall = tl_split_stall;
   const int grid = std::min(ntm * nsc, sms);
   int *rlist = defer ? (int *)(ws + o_rl) : nullptr, *rcount = defer ? (int *)(ws + o_rc) : nullptr;
   cudaError_t e = cudaMemsetAsync(a.next_item, 0, sizeof(int), s);
   if (e == cudaSuccess && defer) e = cudaMemsetAsync(rcount, 0, sizeof(int), s);
   if (e == cudaSuccess) e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
   if (e == cudaSuccess) {
-    split_reduce<<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, a.pskip, u, umap, rlist, rcount);
+    split_reduce<<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, a.pskip, u, umap, rlist, rcount, rowc,
+                                                 anch ? ybar + k : nullptr);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && defer) e = launch_rescue(a, std::max(1, std::min(2 * sms, (m + 7) / 8)), rlist, rcount, u, umap, s);
   if (stream_ordered_alloc) cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_status(e, "split launch");
-  note_launches(defer ? 8 : 7);
+  note_launches((defer ? 8 : 7) + (ff ? (same_pool ? 1 : 2) : 0) + (anch ? 2 : 0));
   return GSKS_OK;
 }
 
@@ -1927,6 +2097,20 @@ __global__ void list_rescue_mark(int ma, int ntask, const int *__restrict__ aoff
     b += pskip[G.pbase + (long long)c * G.m + r];
   }
   if (b > 0.0f && fabs(sum) < 0x1p-69 * (double)b) rlist[atomicAdd(rcount, 1)] = pos;
+}
+
+// Anchored polynomial tasks: each row's v0^p times the task's weight sum
+// (FP64) goes into the row's first chunk partial, before the merge.
+__global__ void list_anchor_add(int ma, int ntask, const int *__restrict__ aoff, const SplitTaskGeo *__restrict__ tg,
+                                const TaskParam *__restrict__ tp, const double *__restrict__ rowc,
+                                const double *__restrict__ wsum, double *__restrict__ partial)
+{
+  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= ma) return;
+  const int t = task_of(aoff, ntask, pos);
+  const SplitTaskGeo G = tg[t];
+  if (!tp[t].anch || G.n <= 0 || G.m <= 0) return;
+  partial[G.pbase + (pos - G.a0)] += rowc[pos] * wsum[t];
 }
 
 __global__ void __launch_bounds__(256) list_rescue(TileArgs a, int ntask, const int *__restrict__ aoff,
@@ -2084,7 +2268,15 @@ int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, con
   Pl.o_ni = Pl.o_rc + al(sizeof(int));
   Pl.o_xaf = Pl.o_ni + al(sizeof(int));
   Pl.o_xbf = Pl.o_xaf + al((size_t)nxa * k * sizeof(float2));
-  const size_t total = Pl.o_xbf + (same_pool ? 0 : al((size_t)nxb * k * sizeof(float2)));
+  // anchored polynomial tasks: per-task source means and weight sums, and the
+  // rows' v0^p
+  Pl.any_anch = false;
+  for (int t = 0; t < ntask && !Pl.any_anch; t++)
+    Pl.any_anch = kps[t].type == KS_POLYNOMIAL && kps[t].pmode == POW_INT && kps[t].pint >= 1 && kps[t].pint <= 4;
+  Pl.o_ybar = Pl.o_xbf + (same_pool ? 0 : al((size_t)nxb * k * sizeof(float2)));
+  Pl.o_wsum = Pl.o_ybar + (Pl.any_anch ? al((size_t)ntask * k * 8) : 0);
+  Pl.o_rowc = Pl.o_wsum + (Pl.any_anch ? al((size_t)ntask * 8) : 0);
+  const size_t total = Pl.o_rowc + (Pl.any_anch ? al((size_t)std::max(Pl.ma, 1) * 8) : 0);
   if (!Pl.ws.ensure(total)) return GSKS_ERR_ALLOC;
   uint8_t *ws = (uint8_t *)Pl.ws.p;
   auto up = [&](size_t off, const void *src, size_t bytes) {
@@ -2128,14 +2320,20 @@ int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int 
     bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(Pl.ma, Pl.mb, k, XA, a_idx, nxa, XB, b_idx, nxb, err,
                                                                bbox);
   }
-  params_kernel<<<1, 1024, 0, s>>>(k, KS_LIST, 0.0, 0.0, tau, bbox, centre, P);
+  params_kernel<<<1, 1024, 0, s>>>(k, KS_LIST, 0.0, 0.0, 0.0, tau, bbox, centre, P);
   task_params_kernel<<<(ntask + 127) / 128, 128, 0, s>>>(ntask, (const KParams *)(ws + Pl.o_kps), P, tau, tp);
+  const SplitTaskGeo *tg = (const SplitTaskGeo *)(ws + Pl.o_tg);
+  double *ybar = Pl.any_anch ? (double *)(ws + Pl.o_ybar) : nullptr;
+  double *wsum = Pl.any_anch ? (double *)(ws + Pl.o_wsum) : nullptr;
+  double *rowc = Pl.any_anch ? (double *)(ws + Pl.o_rowc) : nullptr;
+  if (Pl.any_anch)
+    list_anchor<<<ntask, 256, 256 * sizeof(double), s>>>(ntask, k, tp, tg, XB, b_idx, nxb, w, w_idx, err, ybar, wsum);
   pack_kernel<<<Pl.n_ta, BM, 0, s>>>(0, 0, k, kpad, XA, a_idx, nxa, err, nullptr, nullptr, nullptr, KS_LIST,
                                      centre, P, ws + Pl.o_a, (const int2 *)(ws + Pl.o_ta),
-                                     (const int *)(ws + Pl.o_tat), tp);
+                                     (const int *)(ws + Pl.o_tat), tp, ybar, rowc);
   pack_kernel<<<Pl.n_tb, BN, 0, s>>>(1, 0, k, kpad, XB, b_idx, nxb, err, w, w_idx, nullptr, KS_LIST,
                                      centre, P, ws + Pl.o_b, (const int2 *)(ws + Pl.o_tb),
-                                     (const int *)(ws + Pl.o_tbt), tp);
+                                     (const int *)(ws + Pl.o_tbt), tp, nullptr, nullptr);
   float2 *xaf = (float2 *)(ws + Pl.o_xaf), *xbf = Pl.same_pool ? xaf : (float2 *)(ws + Pl.o_xbf);
   {
     const long long na_c = (long long)nxa * k, nb_c = (long long)nxb * k;
@@ -2154,24 +2352,27 @@ int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int 
   a.pskip = (float *)(ws + Pl.o_pskip);
   a.next_item = (int *)(ws + Pl.o_ni);
   a.err = err;
+  a.wait_limit = tl_split_wait > 0 ? tl_split_wait : WAIT_LIMIT;
+  a.stall = tl_split_stall;
   a.tab = (const SplitItem *)(ws + Pl.o_items);
   a.ntab = Pl.n_items;
   a.tp = tp;
   a.btile_cols = (const int *)(ws + Pl.o_tbc);
   const int grid = std::min(Pl.n_items, sms);
   int *rlist = (int *)(ws + Pl.o_rl), *rcount = (int *)(ws + Pl.o_rc);
-  const SplitTaskGeo *tg = (const SplitTaskGeo *)(ws + Pl.o_tg);
   const int *aoff = (const int *)(ws + Pl.o_aoff);
   cudaError_t e = cudaMemsetAsync(rcount, 0, sizeof(int), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.next_item, 0, sizeof(int), s);
   if (e == cudaSuccess) e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
+  if (e == cudaSuccess && Pl.ma > 0 && Pl.any_anch)
+    list_anchor_add<<<(Pl.ma + 255) / 256, 256, 0, s>>>(Pl.ma, ntask, aoff, tg, tp, rowc, wsum, partial);
   if (e == cudaSuccess && Pl.ma > 0) {
     list_rescue_mark<<<(Pl.ma + 255) / 256, 256, 0, s>>>(Pl.ma, ntask, aoff, tg, partial, a.pskip, rlist, rcount);
     list_rescue<<<std::max(1, std::min(2 * sms, (Pl.ma + 7) / 8)), 256, 0, s>>>(a, ntask, aoff, tg, rlist, rcount);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) return cuda_status(e, "split list launch");
-  *launches += Pl.same_pool ? 10 : 11;
+  *launches += (Pl.same_pool ? 10 : 11) + (Pl.any_anch ? 2 : 0);
   return GSKS_OK;
 }
 
@@ -2179,26 +2380,11 @@ int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int 
 
 using namespace gsks;
 
-// Test hook: one split-precision evaluation (device pointers, Gaussian-type
-// inputs as gsks_dgsks_device) that also writes, for the first tile of CTA 0,
-// the raw accumulators and epilogue values of every (row, column):
-// dump[(row*128 + col)*5 + {0: H, 1: L, 2: K, 3: t, 4: lo}], and the call's
-// scales to params_out (alpha, sigma, inv_sigma, q at byte 0; the centre, k
-// doubles, at byte 64).
-extern "C" int gsks_split_debug_dump(ks_t *kernel, int m, int n, int k, double *u, const int *umap,
-                                     const double *XA, const int *amap, const double *XB, const int *bmap,
-                                     const double *w, const int *wmap, float *dump, void *params_out,
-                                     void *stream)
+// Test hook (gsks.h): the wait limit and the producer stall of this thread's
+// later split-precision calls.
+extern "C" int gsks_split_test_wait(long long wait_cycles, int stall)
 {
-  Ctx *c = get_ctx();
-  if (!c) return gsks_last_error();
-  int st = check_kernel(kernel, k);
-  if (st) return set_status(st, "gsks_split_debug_dump");
-  tl_split_dump = dump;
-  tl_split_params = params_out;
-  st = enqueue_split(c, kernel, m, n, k, u, umap, XA, nullptr, amap, -1, XB, nullptr, bmap, -1, w, wmap,
-                     kernel->hi, kernel->hj, (cudaStream_t)stream, true);
-  tl_split_dump = nullptr;
-  tl_split_params = nullptr;
-  return set_status(st, "gsks_split_debug_dump");
+  tl_split_wait = wait_cycles > 0 ? wait_cycles : 0;
+  tl_split_stall = stall ? 1 : 0;
+  return set_status(GSKS_OK, nullptr);
 }

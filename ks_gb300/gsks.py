@@ -25,6 +25,7 @@ LIB_PATH = os.environ.get("GSKS_LIB", os.path.join(_PKG, "lib", "libgsks.so"))
 KS_GAUSSIAN, KS_POLYNOMIAL, KS_LAPLACE, KS_GAUSSIAN_VAR_BANDWIDTH = 0, 1, 2, 3
 KS_TANH, KS_QUARTIC, KS_MULTIQUADRATIC, KS_EPANECHNIKOV = 4, 5, 6, 7
 GSKS_FP64, GSKS_SPLIT_BF16X3 = 0, 1
+GSKS_ERR_MAP_RANGE, GSKS_ERR_TIMEOUT = 5, 12
 
 # option "type" strings of python/gsks.py:47-79
 TYPE_NAMES = {
@@ -90,6 +91,8 @@ def load():
     lib.gsks_list_plan_errors.argtypes = [vp]
     lib.gsks_list_plan_destroy.restype = C.c_int
     lib.gsks_list_plan_destroy.argtypes = [vp]
+    lib.gsks_split_test_wait.restype = C.c_int
+    lib.gsks_split_test_wait.argtypes = [C.c_longlong, C.c_int]
     _lib = lib
     return lib
 
@@ -109,6 +112,12 @@ def last_launch_count() -> int:
 def device_errors() -> int:
     """Device-side error flags of this thread's context (read and cleared)."""
     return int(load().gsks_device_errors())
+
+
+def split_test_wait(wait_cycles: int = 0, stall: bool = False) -> None:
+    """Test hook: bounded-wait limit (clock cycles, 0 = default) and producer
+    stall of this thread's later split-precision calls (gsks.h)."""
+    load().gsks_split_test_wait(C.c_longlong(int(wait_cycles)), C.c_int(1 if stall else 0))
 
 
 def set_precision(p: int) -> None:

@@ -169,3 +169,33 @@ def test_host_map_negative_index_refused(gpu, which):
             gsks.set_precision(prev)
         assert rc == 5, gsks.error_string(rc)
         assert np.all(u == 2.5)
+
+
+def test_c1_configuration_as_stated(gpu, oracle_mod):
+    """The CPU-runnable configuration exactly: m = n = 2048 targets and sources,
+    k = 16, points U[0,1]^16, norms in FP64, w ~ N(0,1), identity maps,
+    Gaussian h = 1 (scal = -1/(2h^2) = -0.5), seed-generated.  Checked as the
+    reference's own test does (test/test_dgsks.c:41,43-79): the normwise error
+    against dgsks_ref within 1e-13; the split form within its 1e-6 gate."""
+    from ks_gb300 import gsks
+    O = oracle_mod
+    rng = np.random.default_rng(2048)
+    N, k = 2048, 16
+    X = rng.random((N, k))
+    X2 = O.norms(X)
+    w = rng.standard_normal(N)
+    ident = np.arange(N, dtype=np.int32)
+    u_ref = np.zeros(N)
+    O.dgsks(O.make_kernel(0, scal=-0.5), u_ref, ident, X, X2, ident, X, X2, ident, w, ident)
+    _, cond = O.rows(O.make_kernel(0, scal=-0.5), ident, X, X2, ident, X, X2, ident, w, ident)
+    prev = gsks.get_precision()
+    try:
+        for prec, tol in ((gsks.GSKS_FP64, 1e-13), (gsks.GSKS_SPLIT_BF16X3, 1e-6)):
+            gsks.set_precision(prec)
+            u = np.zeros(N)
+            rc = gsks.dgsks_status(gsks.make_kernel(0, scal=-0.5), u, ident, X, X2, ident, X, X2, ident, w, ident)
+            assert rc == 0, gsks.error_string(rc)
+            e = O.errors(u, u_ref, cond=cond)
+            assert e["normwise"] <= tol and e["cond_max"] <= tol, (prec, e)
+    finally:
+        gsks.set_precision(prev)

@@ -188,3 +188,27 @@ def test_split_list_more_items_than_ctas_of_uneven_cost(gpu, oracle_mod):
     specs = _specs(rng, ntask, k, ["gauss", "laplace", "poly"])
     _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True)
     assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
+def test_split_list_polynomial_on_a_constant(gpu, oracle_mod):
+    """Polynomial tasks of powers 1..4 (scal 1/k, cons 1, k = 64, uniform [0, 1])
+    whose weights sum to zero per task: the values sit within a few percent of
+    their mean and sum_j K w_j cancels down to that variation.  Each task's
+    rows are summed around their own anchors (the mean of the task's sources),
+    with the anchors' part added in FP64 per task."""
+    O = oracle_mod
+    rng = np.random.default_rng(41)
+    N, k, ntask = 20000, 64, 8
+    X = rng.random((N, k))
+    sa = rng.integers(200, 600, ntask); sb = rng.integers(1000, 3000, ntask)
+    a_off, a_idx, b_off, b_idx = _lists(rng, N, sa, sb)
+    nb = int(b_off[-1])
+    w = rng.standard_normal(max(N, nb))
+    w_idx = np.arange(nb, dtype=np.int32)                 # every source position its own weight
+    for t in range(ntask):
+        blk = slice(b_off[t], b_off[t + 1])
+        w[blk] -= w[blk].mean()
+    u_idx = np.arange(a_off[-1], dtype=np.int32)          # distinct u entries per task
+    specs = [(1, dict(scal=1.0 / k, cons=1.0, powe=float(1 + t % 4))) for t in range(ntask)]
+    _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True)
+    assert e["normwise"] <= 5e-7 and e["cond_max"] <= 1e-8, e
