@@ -86,6 +86,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_S)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--no-list", action="store_true", help="skip the batched (dgsks_list) section")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations (mixture k=3/512, variable bandwidth, dense k=1024)")
     ap.add_argument("--config", default=None, choices=["c3", "c5a", "c5b"],
                     help="one of the other benchmark configurations instead of the default line: c3 (mixture, "
                          "k swept), c5a (variable bandwidth, 2^20 points), c5b (k = 1024 polynomial)")
@@ -291,29 +293,65 @@ def roofline_split(per, peaks, rates):
     return out
 
 
-def roofline_fp64(per, rates):
+# FP64 pipe: ncu reports sm__inst_executed_pipe_fp64.avg.peak_sustained = 1/16
+# warp instruction per SM cycle on GB300, i.e. 2 DFMA per SM per cycle; the
+# FP64 tensor-core MMA (DMMA) issues to the same pipe at 1.8 FMA per SM cycle
+# (profiles/fp64_pipe_peak.md).
+FP64_FMA_PER_SM_CYCLE = 2.0
+
+
+def fp64_peak(sms, sm_mhz):
+    """FP64 flop/s peak at the sampled SM clock: 2 flops per FMA."""
+    return 2.0 * FP64_FMA_PER_SM_CYCLE * sms * sm_mhz * 1e6
+
+
+def roofline_fp64(per, peak):
+    """FP64 form per kernel: the reference's flop model (2k + f per pair,
+    test/test_dgsks.c:254-283; it counts more flops for pow/exp than binary
+    powering issues, so it can exceed 1) and the rank-k part alone (2k per
+    pair, every one a DFMA: a lower bound of the pipe's load)."""
     out = {}
-    peak = 2.0 * rates["dfma"]
     for name, kt, p, f in KERNELS:
         t = per[name] * 1e-3
         flops = M_T * N_S * (2 * K_DIM + f)
+        rank_k = M_T * N_S * 2 * K_DIM
         out[name] = {"ms": round(per[name], 3), "pairs_per_s": M_T * N_S / t,
-                     "achieved_tflops": round(flops / t / 1e12, 4), "frac": round(flops / t / peak, 4)}
+                     "achieved_tflops": round(flops / t / 1e12, 4), "frac": round(flops / t / peak, 4),
+                     "frac_rank_k": round(rank_k / t / peak, 4)}
     return out
 
 
-def read_traffic(name):
-    """DRAM bytes per launch from a committed ncu summary (profiles/<name>.md)."""
+def read_profile_value(name, key):
+    """A `key: value` line of a committed ncu summary (profiles/<name>.md)."""
     path = os.path.join(ROOT, "profiles", name + ".md")
     if not os.path.exists(path):
         return None
     for l in open(path):
-        if l.startswith("traffic_bytes_per_launch:"):
+        if l.startswith(key + ":"):
             try:
                 return float(l.split(":", 1)[1])
             except ValueError:
                 return None
     return None
+
+
+def read_traffic(name):
+    """DRAM bytes per launch from a committed ncu summary."""
+    return read_profile_value(name, "traffic_bytes_per_launch")
+
+
+def issue_bound(name, pairs, t, sm_mhz, sms):
+    """Issue-rate bound of a kernel: its thread instructions per pair (ncu,
+    committed summary) x pairs over the issue capacity, one warp instruction
+    per cycle per SM sub-partition (SMs x 4 x clock x 32 threads)."""
+    ipp = read_profile_value(name, "thread_instructions_per_pair")
+    if ipp is None or not sm_mhz:
+        return None
+    cap = sms * 4 * sm_mhz * 1e6 * 32
+    t_issue = ipp * pairs / cap
+    return {"thread_instructions_per_pair": ipp, "capacity_thread_instr_per_s": cap,
+            "t_issue_ms": round(t_issue * 1e3, 4), "frac": round(t_issue / t, 4),
+            "source": f"profiles/{name}.md (ncu smsp__inst_executed.sum x 32 / pairs)"}
 
 
 def run_ours(args, ws, rank, local):
@@ -329,20 +367,25 @@ def run_ours(args, ws, rank, local):
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     peaks = peaks_file()
     rates = {}
-    for nm, w in (("dfma", 0), ("ffma", 1), ("ex2", 2)):
+    for nm, w in (("dfma", 0), ("ffma", 1), ("ex2", 2), ("dmma", 3)):
         r = C.c_double()
         lib.gsks_probe_peak(w, C.byref(r))
         rates[nm] = r.value
 
     clk = ClockSampler(local)
-    results = {}
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    results, pers = {}, {}
     for form in forms:
         ms, per, launches = time_form(args, torch, gsks, wl, form, ws, flush, stream, clk)
         pairs_step = len(KERNELS) * M_T * N_S
+        pers[form] = per
         results[form] = {"value": pairs_step * args.steps * ws / (ms * 1e-3), "ms_per_step": ms / args.steps,
-                         "gpu_launches": launches,
-                         "per_kernel": roofline_split(per, peaks, rates) if form == "split"
-                         else roofline_fp64(per, rates)}
+                         "gpu_launches": launches}
+    sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+    p64 = fp64_peak(sms, sm_mhz)
+    for form in forms:
+        results[form]["per_kernel"] = (roofline_split(pers[form], peaks, rates) if form == "split"
+                                       else roofline_fp64(pers[form], p64))
     head = forms[0]
     H = results[head]
 
@@ -360,9 +403,18 @@ def run_ours(args, ws, rank, local):
                 if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s bf16"}
     else:
         roof = {"bound": "fp64", "kernel": f"fp64_tiles<{dom}>", "achieved": dk["achieved_tflops"],
-                "peak": round(2 * rates["dfma"] / 1e12, 4), "unit": "TFLOP/s", "frac": dk["frac"],
+                "peak": round(p64 / 1e12, 4), "unit": "TFLOP/s", "frac": dk["frac"],
                 "traffic": read_traffic(f"fp64_tiles_{dom}_general_stride"),
-                "peak_source": "measured live: gsks_probe_peak FP64 FMA rate x 2"}
+                "peak_source": "FP64 pipe issue rate (ncu peak_sustained: 2 DFMA per SM cycle) x SMs x the "
+                               "median SM clock sampled in the timed region"}
+    roof["fp64_peak_tflops"] = round(p64 / 1e12, 4)
+    roof["fp64_peak_source"] = ("2 DFMA per SM cycle (ncu sm__inst_executed_pipe_fp64 peak_sustained) x "
+                                f"{sms} SMs x {sm_mhz:.0f} MHz (median sampled); live probes: DFMA chains "
+                                f"{rates['dfma']:.3g} FMA/s, DMMA {rates.get('dmma', 0):.3g} FMA/s")
+    if head == "split":
+        ib = issue_bound(f"split_tiles_{dom}_general_stride", M_T * N_S, dk["ms"] * 1e-3, sm_mhz, sms)
+        if ib:
+            roof["issue"] = ib
     roof["per_form"] = {f: results[f]["per_kernel"] for f in forms}
     roof["pipe_rates_measured"] = {k: float("%.4g" % v) for k, v in rates.items()}
 
@@ -396,6 +448,9 @@ def run_ours(args, ws, rank, local):
         del wl
         torch.cuda.empty_cache()
         line["list"] = run_list(args, torch, gsks, forms)
+    if not args.no_configs and ws == 1:
+        torch.cuda.empty_cache()
+        line["configs"] = run_configs_default(args, torch, gsks)
     return line
 
 
@@ -789,27 +844,21 @@ def _config_data(torch, name, k, m, seed):
     return X.contiguous(), w, kernels, extra
 
 
-def run_config(args):
+def config_results(args, torch, gsks, O, cname, ks, clk, flush, steps, warmup):
+    """One configuration at full size: per k and kernel, the split form over all
+    m*n pairs (median of `steps` calls, L2 flushed before each), the FP64 form
+    on a block of target rows x all sources (about 0.3 s), and both forms'
+    errors on 256 sampled rows against the oracle.  Both forms are timed
+    inside the clock sampler `clk`."""
     import numpy as np
-    import torch
-    from ks_gb300 import build as B
-    if not os.path.exists(B.LIB):
-        B.build()
-    from ks_gb300 import gsks
-    from oracle import oracle as O
-    torch.cuda.set_device(0)
-    spec = CONFIG_SPECS[args.config]
+    spec = CONFIG_SPECS[cname]
     m = spec["m"]
     stream = torch.cuda.current_stream()
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     peaks = peaks_file()
     tc_peak = peaks.get("bf16_tflops", 1900.0) * 1e12
-    O.build()
-    O.set_threads(os.cpu_count() or 1)
     results = []
-    clk = ClockSampler(0)
-    for k in spec["ks"]:
-        X, w, kernels, extra = _config_data(torch, args.config, k, m, 1000 + k)
+    for k in ks:
+        X, w, kernels, extra = _config_data(torch, cname, k, m, 1000 + k)
         X2 = torch.empty(m, dtype=torch.float64, device="cuda")
         gsks.norms_device(X, X2, stream=stream)
         ident = torch.arange(m, dtype=torch.int32, device="cuda")
@@ -826,13 +875,13 @@ def run_config(args):
 
             # split over all pairs
             u = torch.zeros(m, dtype=torch.float64, device="cuda")
-            for _ in range(max(1, args.warmup)):
+            for _ in range(max(1, warmup)):
                 call(u, ident, gsks.GSKS_SPLIT_BF16X3)
             u.zero_()
             torch.cuda.synchronize()
             ts = []
             with clk:
-                for _ in range(args.steps):
+                for _ in range(steps):
                     flush.zero_()
                     a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
                     a.record(stream)
@@ -842,21 +891,24 @@ def run_config(args):
                     ts.append(a.elapsed_time(b))
             t_split = statistics.median(ts) * 1e-3
             pairs = float(m) * m
-            u_split = (u / args.steps).cpu().numpy()
-            # FP64 on a block of rows sized to about half a second
-            est = 1.06e12 / (2 * k + 40)
-            mr = int(min(m, max(152 * 2 * 64, est * 0.5 / m)))
+            u_split = (u / steps).cpu().numpy()
+            # FP64 on a block of rows sized to about 0.3 s (at least 1024 rows: the
+            # plan splits the sources into chunks, so every SM stays busy)
+            est = 5.9e11 / (k + 12)
+            mr = int(min(m, max(1024, est * 0.3 / m)))
             mr = (mr // 64) * 64
             rows = torch.randperm(m, device="cuda")[:mr].to(torch.int32).sort().values
             uf = torch.zeros(m, dtype=torch.float64, device="cuda")
             call(uf, rows[:64], gsks.GSKS_FP64)
             uf.zero_()
             torch.cuda.synchronize()
-            a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            call(uf, rows, gsks.GSKS_FP64)
-            b.record(stream)
-            torch.cuda.synchronize()
+            with clk:
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True); b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                call(uf, rows, gsks.GSKS_FP64)
+                b.record(stream)
+                torch.cuda.synchronize()
             t_fp64 = a.elapsed_time(b) * 1e-3
             fp64_rate = float(mr) * m / t_fp64
             # errors on sampled rows of the FP64 block
@@ -876,22 +928,66 @@ def run_config(args):
             err = {"split": {kk: float("%.3g" % v) for kk, v in O.errors(u_split[sample], ref, cond=cond).items()},
                    "fp64": {kk: float("%.3g" % v) for kk, v in O.errors(ufh[sample], ref, cond=cond).items()}}
             alg = 2.0 * pairs * k
+            sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+            p64 = fp64_peak(sms, clk.summary().get("sm_mhz") or 2070.0)
             results.append({"k": k, "kernel": name, "pairs": pairs,
                             "split": {"value": pairs / t_split, "ms": round(t_split * 1e3, 3),
                                       "alg_tflops": round(alg / t_split / 1e12, 2),
                                       "frac_alg_tensor": round(alg / tc_peak / t_split, 4)},
-                            "fp64": {"value": fp64_rate, "rows_timed": mr, "ms": round(t_fp64 * 1e3, 2)},
+                            "fp64": {"value": fp64_rate, "rows_timed": mr, "ms": round(t_fp64 * 1e3, 2),
+                                     "frac_rank_k": round(2.0 * k * fp64_rate / p64, 4)},
                             "split_over_fp64": (pairs / t_split) / fp64_rate,
                             "error": err, "rows_checked": int(sample.size)})
             del u, uf
         del X, X2, w, ident
         torch.cuda.empty_cache()
+    return results
+
+
+CONFIG_TIMING = ("split: CUDA events per call over all m*n pairs, median of the timed steps, L2 flushed before "
+                 "each; fp64: one call over a block of target rows x all sources, L2 flushed before it")
+
+
+def run_config(args):
+    import torch
+    from ks_gb300 import build as B
+    if not os.path.exists(B.LIB):
+        B.build()
+    from ks_gb300 import gsks
+    from oracle import oracle as O
+    torch.cuda.set_device(0)
+    spec = CONFIG_SPECS[args.config]
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    clk = ClockSampler(0)
+    results = config_results(args, torch, gsks, O, args.config, spec["ks"], clk, flush, args.steps, args.warmup)
     line = {"metric": METRIC, "unit": "pair-evals/s", "config": {"workload": spec["desc"], "name": args.config},
             "steps": args.steps, "warmup": args.warmup, "data": "synthetic, seeded (torch generator on the device)",
-            "timing": "split: CUDA events per call over all m*n pairs, median of the timed steps, L2 flushed "
-                      "before each; fp64: one call over a block of target rows x all sources",
-            "results": results, "clocks": clk.summary()}
+            "timing": CONFIG_TIMING, "results": results, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
+
+
+# The other configurations carried by the default line (key "configs"): the
+# mixture at its smallest and largest k, the variable-bandwidth and the dense
+# configuration, all at full size.
+DEFAULT_CONFIGS = [("c3", [3, 512]), ("c5a", [8]), ("c5b", [1024])]
+
+
+def run_configs_default(args, torch, gsks):
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    clk = ClockSampler(0)
+    steps = max(1, min(args.steps, 3))
+    out = {"timing": CONFIG_TIMING, "steps": steps, "warmup": 1,
+           "data": "synthetic, seeded (torch generator on the device)"}
+    for cname, ks in DEFAULT_CONFIGS:
+        out[cname] = {"workload": CONFIG_SPECS[cname]["desc"],
+                      "results": config_results(args, torch, gsks, O, cname, ks, clk, flush, steps, 1)}
+    out["clocks"] = clk.summary()
+    return out
 
 
 def main():

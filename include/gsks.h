@@ -169,8 +169,9 @@ int gsks_device_errors(void);
 /* ---- calibration -------------------------------------------------------- */
 /* Measured issue rate of one pipe of the current device, in operations per
  * second (an FMA counts as one operation): what = 0 FP64 FMA, 1 FP32 FMA,
- * 2 SFU ex2.  Used for the roofline fractions the benchmark reports; the
- * reference has no counterpart. */
+ * 2 SFU ex2, 3 FP64 tensor-core FMA (DMMA, mma.sync m8n8k4).  Used for the
+ * roofline fractions the benchmark reports; the reference has no
+ * counterpart. */
 int gsks_probe_peak(int what, double *ops_per_s);
 
 /* ---- diagnostics -------------------------------------------------------- */

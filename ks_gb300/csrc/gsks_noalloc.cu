@@ -98,7 +98,9 @@ extern "C" int gsks_dgsks_device_noalloc(ks_t *kernel, int m, int n, int k,
   if ((st = noalloc_setup(d)) != GSKS_OK) return st;
 
   // Same decomposition as gsks_dgsks_device, with the number of source chunks
-  // capped so that chunks x rows fits the array.
+  // capped so that chunks x rows fits the array.  fp64_plan keeps nsc * ntm
+  // below 32 * SMs + ntm (or nsc = 1), i.e. under 2^20 partials for up to 256
+  // SMs (GB300 has 152): the cap is a guard for larger devices.
   Fp64Plan p = fp64_plan(m, n, k, d->num_sms);
   if (p.partial_elems > NOALLOC_MAX_PARTIAL) {
     const long long nsc_max = std::max<long long>(1, (long long)(NOALLOC_MAX_PARTIAL / (size_t)p.ldp));

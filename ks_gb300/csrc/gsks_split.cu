@@ -476,13 +476,24 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   out[t] = T;
 }
 
-// Float-pair copy of a pool: Xf[i] = (hi, lo), hi + lo = X[i] to 2^-48.  With
-// P != nullptr (a single call) only when the call may flag pairs.
-__global__ void pool_split(long long n, const double *__restrict__ X, float2 *__restrict__ Xf, const Params *P)
+// Float-pair copy of n / k points: Xf[i] = (hi, lo), hi + lo = the
+// coordinate to 2^-48.  Without a map, of the pool's first points; with one
+// (a single call's gathered rows), row r of the copy is pool point map[r]
+// (entries outside [0, npool), npool >= 0, read point 0).  With P != nullptr
+// (a single call) only when the call may flag pairs.
+__global__ void pool_split(long long n, int k, const double *__restrict__ X, const int *__restrict__ map, int npool,
+                           float2 *__restrict__ Xf, const Params *P)
 {
   if (P && !P->any_flag) return;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)blockDim.x * gridDim.x) {
-    const double v = X[i];
+    size_t src = (size_t)i;
+    if (map) {
+      const long long r = i / k;
+      int p = map[r];
+      if (npool >= 0 && (p < 0 || p >= npool)) p = 0;
+      src = (size_t)p * k + (size_t)(i - r * k);
+    }
+    const double v = X[src];
     const float h = (float)v;
     Xf[i] = make_float2(h, (float)(v - (double)h));
   }
@@ -521,28 +532,61 @@ __device__ void block_source_sums(int j0, int j1, int k, const double *__restric
   }
 }
 
-// Anchor point of a single call's polynomial kernel: the mean of the gathered
-// sources, and the sum of their weights.  Pass 1: block b sums its range of
-// sources into part[b * (k + 1) ..]; pass 2 (one block) adds the blocks in order.
-__global__ void anchor_partial(int n, int k, const double *__restrict__ XB, const int *__restrict__ bmap, int nxb,
-                               const double *__restrict__ w, const int *__restrict__ wmap, int *err,
-                               double *__restrict__ part)
+// Anchor point of a single call's polynomial kernel and the sum of all
+// weights.  Any point inside the sources' hull keeps each row's anchor value
+// within the range of that row's values, so the mean of a strided sample of
+// at most ANCHOR_SAMPLE sources serves (blocks 0 .. ceil(k/32)-1: 32
+// coordinates each, 8 warps over the sample, combined in warp order).  The
+// weight sum covers every source (blocks from ceil(k/32) on: contiguous
+// ranges, fixed-order tree; anchor_final adds the ranges in order).  All of
+// it deterministic.
+constexpr int ANCHOR_SAMPLE = 2048;
+constexpr int ANCHOR_WPER = 4096;   // weights per block of the weight sum
+
+__global__ void __launch_bounds__(256) anchor_partial(int n, int k, const double *__restrict__ XB,
+                                                      const int *__restrict__ bmap, int nxb,
+                                                      const double *__restrict__ w, const int *__restrict__ wmap,
+                                                      int *err, double *__restrict__ ybar,
+                                                      double *__restrict__ wpart)
 {
-  extern __shared__ double sh_sum[];
-  const int per = (n + gridDim.x - 1) / gridDim.x;
-  const int j0 = min(n, blockIdx.x * per), j1 = min(n, j0 + per);
-  double *out = part + (size_t)blockIdx.x * (k + 1);
-  block_source_sums(j0, j1, k, XB, bmap, nxb, err, w, wmap, 1.0, out, out + k, sh_sum);
+  __shared__ double sh[256];
+  const int ncb = (k + 31) / 32, t = threadIdx.x, lane = t & 31, wp = t >> 5;
+  if ((int)blockIdx.x < ncb) {
+    const int S = min(n, ANCHOR_SAMPLE), stride = n / S;
+    const int p = blockIdx.x * 32 + lane;
+    double s = 0.0;
+    if (p < k) {
+#pragma unroll 4
+      for (int q = wp; q < S; q += 8) s += XB[(size_t)pool_index(bmap, q * stride, nxb, err) * k + p];
+    }
+    sh[t] = s;
+    __syncthreads();
+    if (wp == 0 && p < k) {
+      double r = 0.0;
+      for (int q = 0; q < 8; q++) r += sh[q * 32 + lane];
+      ybar[p] = r / (double)S;
+    }
+    return;
+  }
+  const int b = blockIdx.x - ncb;
+  const int j0 = b * ANCHOR_WPER, j1 = min(n, j0 + ANCHOR_WPER);
+  double s = 0.0;
+  for (int j = j0 + t; j < j1; j += 256) s += w[wmap ? wmap[j] : j];
+  sh[t] = s;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (t < h) sh[t] += sh[t + h];
+    __syncthreads();
+  }
+  if (t == 0) wpart[b] = sh[0];
 }
 
-__global__ void anchor_final(int nblk, int n, int k, const double *__restrict__ part, double *__restrict__ ybar,
-                             double *__restrict__ wsum)
+__global__ void anchor_final(int nwb, const double *__restrict__ wpart, double *__restrict__ wsum)
 {
-  for (int p = threadIdx.x; p <= k; p += blockDim.x) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0.0;
-    for (int b = 0; b < nblk; b++) s += part[(size_t)b * (k + 1) + p];
-    if (p < k) ybar[p] = s / (double)n;
-    else *wsum = s;
+    for (int b = 0; b < nwb; b++) s += wpart[b];
+    *wsum = s;
   }
 }
 
@@ -716,7 +760,8 @@ struct TileArgs {
   int ntm, ntn, nsc, chunk_tiles;   // items = ntm * nsc; chunk = source tiles per item
   const uint8_t *imgA, *imgB;
   const double *XA, *XB;            // pool coordinates (FP64) for the rechecks
-  const float2 *XAf, *XBf;          // list form: the pools as float pairs (or nullptr)
+  const float2 *XAf, *XBf;          // float-pair copies for the rechecks (or nullptr)
+  int ffpos;                        // the copies are indexed by position (else by pool point)
   const int *amap, *bmap, *wmap;
   int nxa, nxb;                     // pool sizes for the map range checks (-1: unchecked)
   const double *w;
@@ -1054,7 +1099,8 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
                 KT == KS_LAPLACE) {
     if (a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag)) {   // the copies exist
       // (a single call builds them only when it may flag pairs)
-      const float2 *x = a.XAf + (size_t)pa * a.k, *y = a.XBf + (size_t)pb * a.k;
+      const float2 *x = a.XAf + (size_t)(a.ffpos ? ipos : pa) * a.k;
+      const float2 *y = a.XBf + (size_t)(a.ffpos ? jpos : pb) * a.k;
       double hf = 0.0;
       if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) hf = T.kp.hi[pa] * T.kp.hj[pb];
       if constexpr (PRE && KT != KS_LAPLACE) {
@@ -1103,7 +1149,7 @@ __device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T
   if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
   if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
   float th, tl;
-  ff_dist2(a.XAf + (size_t)pa * a.k, a.XBf + (size_t)pb * a.k, a.k, th, tl);
+  ff_dist2(a.XAf + (size_t)(a.ffpos ? ipos : pa) * a.k, a.XBf + (size_t)(a.ffpos ? jpos : pb) * a.k, a.k, th, tl);
   float ph, pl;
   if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
     // (-0.5 log2e hi) hj from the row's and the column's float pairs
@@ -1965,11 +2011,14 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const size_t o_a = o_bbox + al((size_t)2 * k * 8);
   const size_t o_b = o_a + al((size_t)ntm * tile_bytes(BM, kpad));
   const size_t o_p = o_b + al((size_t)ntn * tile_bytes(BN, kpad));
-  // float-pair copies of the pools for cheap rechecks, when the pools are known
-  // and not much larger than the gathered points
+  // float-pair copies for cheap rechecks (kernels with rechecks; written only
+  // when the call may flag pairs): of the pool when the targets and sources
+  // share one whose points are no more than the gathered ones (indexed by
+  // pool point), else of the gathered rows (indexed by position)
   const bool same_pool = XA == XB && nxa == nxb;
-  const long long pool_pts = nxa < 0 || nxb < 0 ? -1 : (long long)nxa + (same_pool ? 0 : nxb);
-  const bool ff = kt_rescue(ker->type) && pool_pts >= 0 && pool_pts <= std::max(4LL * (m + n), 1LL << 22);
+  const bool ff = kt_rescue(ker->type);
+  const bool ffpos = !(same_pool && nxa >= 0 && (long long)nxa <= (long long)m + n);
+  const long long ffa = ffpos ? m : nxa, ffb = ffpos ? n : (same_pool ? 0 : nxb);   // points per copy
   // row rescue (exponential kernels): skipped-group weights, row list, count
   const bool defer = kt_rescue(ker->type);
   const size_t o_ps = o_p + al((size_t)nsc * ldp * 8);
@@ -1977,14 +2026,14 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const size_t o_rc = o_rl + (defer ? al((size_t)m * 4) : 0);
   const size_t o_ni = o_rc + (defer ? al(4) : 0);   // work counter
   const size_t o_xaf = o_ni + al(4);
-  const size_t o_xbf = o_xaf + (ff ? al((size_t)nxa * k * sizeof(float2)) : 0);
+  const size_t o_xbf = o_xaf + (ff ? al((size_t)ffa * k * sizeof(float2)) : 0);
   // anchored polynomial: source mean and weight sum (ybar | wsum | block
   // partials) and the rows' v0^p
   const bool anch = ker->type == KS_POLYNOMIAL && ker->powe == rint(ker->powe) && ker->powe >= 1.0 &&
                     ker->powe <= 4.0;
-  const int nab = std::max(1, std::min(sms, (n + 255) / 256));   // blocks of the first anchor pass
-  const size_t o_anc = o_xbf + (ff && !same_pool ? al((size_t)nxb * k * sizeof(float2)) : 0);
-  const size_t o_rowc = o_anc + (anch ? al(((size_t)k + 1 + (size_t)nab * (k + 1)) * 8) : 0);
+  const int nwb = (n + ANCHOR_WPER - 1) / ANCHOR_WPER;   // blocks of the weight sum
+  const size_t o_anc = o_xbf + (ff ? al((size_t)ffb * k * sizeof(float2)) : 0);
+  const size_t o_rowc = o_anc + (anch ? al(((size_t)k + 1 + (size_t)nwb) * 8) : 0);
   const size_t total = o_rowc + (anch ? al((size_t)m * 8) : 0);
   uint8_t *ws = nullptr;
   if (stream_ordered_alloc) {
@@ -2013,10 +2062,10 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   params_kernel<<<1, 1024, 0, s>>>(k, ker->type, ker->scal, ker->cons, ker->powe, tau, bbox, centre, P);
   double *ybar = anch ? (double *)(ws + o_anc) : nullptr;
   double *rowc = anch ? (double *)(ws + o_rowc) : nullptr;
-  if (anch) {
-    double *part = ybar + k + 1;
-    anchor_partial<<<nab, 256, 256 * sizeof(double), s>>>(n, k, XB, bmap, nxb, w, wmap, err_word(c), part);
-    anchor_final<<<1, 256, 0, s>>>(nab, n, k, part, ybar, ybar + k);
+  if (anch) {   // ybar[k] | wsum | the weight-sum blocks' partials
+    anchor_partial<<<(k + 31) / 32 + nwb, 256, 0, s>>>(n, k, XB, bmap, nxb, w, wmap, err_word(c), ybar,
+                                                      ybar + k + 1);
+    anchor_final<<<1, 32, 0, s>>>(nwb, ybar + k + 1, ybar + k);
   }
   pack_kernel<<<ntm, BM, 0, s>>>(0, m, k, kpad, XA, amap, nxa, err_word(c), nullptr, nullptr, hi, ker->type,
                                  centre, P, ws + o_a, nullptr, nullptr, nullptr, ybar, rowc);
@@ -2030,13 +2079,17 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   a.XA = XA; a.XB = XB; a.amap = amap; a.bmap = bmap; a.wmap = wmap; a.w = w;
   a.nxa = nxa; a.nxb = nxb;
   a.hi = hi; a.hj = hj;
+  int ff_launches = 0;
   if (ff) {
-    float2 *xaf = (float2 *)(ws + o_xaf), *xbf = same_pool ? xaf : (float2 *)(ws + o_xbf);
-    const long long na_c = (long long)nxa * k, nb_c = (long long)nxb * k;
-    pool_split<<<(int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1), 256, 0, s>>>(na_c, XA, xaf, P);
-    if (!same_pool)
-      pool_split<<<(int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1), 256, 0, s>>>(nb_c, XB, xbf, P);
+    float2 *xaf = (float2 *)(ws + o_xaf), *xbf = ffb == 0 ? xaf : (float2 *)(ws + o_xbf);
+    const long long na_c = ffa * k, nb_c = ffb * k;
+    const int ga = (int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1);
+    const int gb = (int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1);
+    pool_split<<<ga, 256, 0, s>>>(na_c, k, XA, ffpos ? amap : nullptr, nxa, xaf, P);
+    ff_launches = 1;
+    if (ffb) { pool_split<<<gb, 256, 0, s>>>(nb_c, k, XB, ffpos ? bmap : nullptr, nxb, xbf, P); ff_launches = 2; }
     a.XAf = xaf; a.XBf = xbf;
+    a.ffpos = ffpos ? 1 : 0;
   }
   a.kp = make_kparams(ker, hi, hj);
   a.kp.coinc = coincidence_eps(k);
@@ -2061,7 +2114,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   if (e == cudaSuccess && defer) e = launch_rescue(a, std::max(1, std::min(2 * sms, (m + 7) / 8)), rlist, rcount, u, umap, s);
   if (stream_ordered_alloc) cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_status(e, "split launch");
-  note_launches((defer ? 8 : 7) + (ff ? (same_pool ? 1 : 2) : 0) + (anch ? 2 : 0));
+  note_launches((defer ? 8 : 7) + ff_launches + (anch ? 2 : 0));
   return GSKS_OK;
 }
 
@@ -2337,9 +2390,11 @@ int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int 
   float2 *xaf = (float2 *)(ws + Pl.o_xaf), *xbf = Pl.same_pool ? xaf : (float2 *)(ws + Pl.o_xbf);
   {
     const long long na_c = (long long)nxa * k, nb_c = (long long)nxb * k;
-    pool_split<<<(int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1), 256, 0, s>>>(na_c, XA, xaf, nullptr);
+    pool_split<<<(int)std::min<long long>(8LL * sms, (na_c + 255) / 256 + 1), 256, 0, s>>>(na_c, k, XA, nullptr, -1, xaf,
+                                                                                        nullptr);
     if (!Pl.same_pool)
-      pool_split<<<(int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1), 256, 0, s>>>(nb_c, XB, xbf, nullptr);
+      pool_split<<<(int)std::min<long long>(8LL * sms, (nb_c + 255) / 256 + 1), 256, 0, s>>>(nb_c, k, XB, nullptr, -1,
+                                                                                          xbf, nullptr);
   }
   TileArgs a{};
   a.k = k; a.kpad = kpad; a.kt = KS_LIST;

@@ -86,13 +86,31 @@ def _compile(src, out, cxx):
     subprocess.run(cmd, check=True, capture_output=True)
 
 
-def test_c_caller_links_unchanged(gpu, tmp_path):
+def test_c_caller_links_unchanged(gpu, oracle_mod, tmp_path):
     exe = str(tmp_path / "link_dgsks")
     _compile(os.path.join(ROOT, "tests", "c", "link_dgsks.c"), exe, "gcc")
     out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()
     vals = np.array(out, dtype=np.float64).reshape(-1, 2)
     assert np.abs(vals[:, 0]).max() > 0
-    assert np.linalg.norm(vals[:, 0] - vals[:, 1]) <= 1e-12 * np.linalg.norm(vals[:, 1])
+    # the program's inputs (its LCG and formulas), then the oracle's dgsks_ref
+    O = oracle_mod
+    N, K, M, NS = 300, 9, 120, 100
+    X = np.empty(N * K)
+    s = 12345
+    for i in range(N * K):
+        s = (s * 1103515245 + 12345) & 0xFFFFFFFF
+        X[i] = ((s >> 8) % 1000) / 1000.0
+    X = X.reshape(N, K)
+    X2 = O.norms(X)
+    w = ((np.arange(N) * 37) % 17) / 17.0 - 0.5
+    amap = ((np.arange(M) * 7) % N).astype(np.int32)
+    umap = ((np.arange(M) * 11) % N).astype(np.int32)
+    bmap = ((np.arange(NS) * 13 + 5) % N).astype(np.int32)
+    wmap = ((np.arange(NS) * 3 + 1) % N).astype(np.int32)
+    u_ref = np.zeros(N)
+    O.dgsks(O.make_kernel(0, scal=-0.5), u_ref, umap, X, X2, amap, X, X2, bmap, w, wmap)
+    for col in range(2):   # dgsks() and dgsks_ref() as the program linked them
+        assert np.linalg.norm(vals[:, col] - u_ref) <= 1e-12 * np.linalg.norm(u_ref), col
 
 
 def test_cpp_list_caller_links_unchanged(gpu, oracle_mod, tmp_path):
