@@ -892,6 +892,7 @@ def config_results(args, torch, gsks, O, cname, ks, clk, flush, steps, warmup):
             t_split = statistics.median(ts) * 1e-3
             pairs = float(m) * m
             u_split = (u / steps).cpu().numpy()
+            stats = gsks.split_stats()
             # FP64 on a block of rows sized to about 0.3 s (at least 1024 rows: the
             # plan splits the sources into chunks, so every SM stays busy)
             est = 5.9e11 / (k + 12)
@@ -933,7 +934,9 @@ def config_results(args, torch, gsks, O, cname, ks, clk, flush, steps, warmup):
             results.append({"k": k, "kernel": name, "pairs": pairs,
                             "split": {"value": pairs / t_split, "ms": round(t_split * 1e3, 3),
                                       "alg_tflops": round(alg / t_split / 1e12, 2),
-                                      "frac_alg_tensor": round(alg / tc_peak / t_split, 4)},
+                                      "frac_alg_tensor": round(alg / tc_peak / t_split, 4),
+                                      "rechecked_pairs": stats["rechecked_pairs"],
+                                      "rescued_rows": stats["rescued_rows"]},
                             "fp64": {"value": fp64_rate, "rows_timed": mr, "ms": round(t_fp64 * 1e3, 2),
                                      "frac_rank_k": round(2.0 * k * fp64_rate / p64, 4)},
                             "split_over_fp64": (pairs / t_split) / fp64_rate,

@@ -175,6 +175,14 @@ int gsks_device_errors(void);
 int gsks_probe_peak(int what, double *ops_per_s);
 
 /* ---- diagnostics -------------------------------------------------------- */
+/* Counts of the calling thread's last single split-precision evaluation
+ * (dgsks / gsks_dgsks_device with GSKS_SPLIT_BF16X3; not dgsks_list): the
+ * pairs whose kernel value an error bound sent to a recheck from the pool
+ * coordinates, and the target rows redone in full because all their values
+ * lay below the FP32 range.  Waits for the device.  No counterpart in the
+ * reference. */
+int gsks_split_stats(long long *rechecked_pairs, int *rescued_rows);
+
 /* Test hook of the split-precision form (no counterpart in the reference).
  * Sets, for the calling thread's later split-precision calls (dgsks,
  * dgsks_status, gsks_dgsks_device, dgsks_list, ...), the limit of the

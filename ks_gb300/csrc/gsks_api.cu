@@ -86,7 +86,7 @@ Ctx::~Ctx()
 {
   // Runs at host-thread exit; the CUDA runtime may already be gone at
   // process teardown, in which case the frees fail harmlessly.
-  for (DevBuf *b : {&partial, &err, &dA, &dA2, &dB, &dB2, &dw, &du, &dhi, &dhj, &dwork, &rmaps, &serr})
+  for (DevBuf *b : {&partial, &err, &dA, &dA2, &dB, &dB2, &dw, &du, &dhi, &dhj, &dwork, &rmaps, &serr, &stats})
     b->release();
   for (PinBuf *b : {&hA, &hA2, &hB, &hB2, &hw, &hu, &hhi, &hhj}) b->release();
   if (stream) cudaStreamDestroy(stream);

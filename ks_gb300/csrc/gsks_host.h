@@ -31,6 +31,7 @@ struct Ctx {
   DevBuf dA, dA2, dB, dB2, dw, du, dhi, dhj, dwork;
   DevBuf rmaps;                // per-rhs u and w maps of the multi-rhs calls
   DevBuf serr;                 // synchronous calls: [0] device error flags, [1] sgsks map-check flag
+  DevBuf stats;                // the last split-precision call: rechecked pairs (u64), rescued rows (int)
   int *cur_err = nullptr;      // the error word kernels write (nullptr: err, the asynchronous calls')
   PinBuf hA, hA2, hB, hB2, hw, hu, hhi, hhj;
   ~Ctx();

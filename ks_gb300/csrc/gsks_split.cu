@@ -762,6 +762,7 @@ struct TileArgs {
   const double *XA, *XB;            // pool coordinates (FP64) for the rechecks
   const float2 *XAf, *XBf;          // float-pair copies for the rechecks (or nullptr)
   int ffpos;                        // the copies are indexed by position (else by pool point)
+  unsigned long long *nrecheck;     // count of rechecked pairs (or nullptr)
   const int *amap, *bmap, *wmap;
   int nxa, nxb;                     // pool sizes for the map range checks (-1: unchecked)
   const double *w;
@@ -1056,29 +1057,54 @@ __device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb
   return kv * wv;
 }
 
-// Squared distance of two points given as float pairs: TwoSum per coordinate
-// difference, exact square by FMA, TwoSum accumulation (about 2^-44 relative),
-// returned as the float pair th + tl.
+// One coordinate of a float-pair squared distance: (u - v)^2 added to the
+// double-float (sh, sl) by a TwoSum difference, an exact square by FMA and a
+// TwoSum accumulation.
+__device__ __forceinline__ void ff_acc(float2 u, float2 v, float &sh, float &sl)
+{
+  const float s = u.x - v.x;                       // TwoSum(u.x, -v.x)
+  const float bv = s - u.x;
+  float e = (u.x - (s - bv)) + (-v.x - bv);
+  e += u.y - v.y;
+  const float dh = s + e, dl = e - (dh - s);       // Fast2Sum
+  const float q = dh * dh;
+  const float qe = fmaf(dh, dh, -q) + 2.f * dh * dl;
+  const float t = sh + q;                          // TwoSum(sh, q)
+  const float z = t - sh;
+  sl += ((sh - (t - z)) + (q - z)) + qe;
+  sh = t;
+}
+
+// Squared distance of two points given as float pairs (about 2^-44
+// relative), returned as the float pair th + tl.  Even and odd coordinates go
+// to two accumulators, combined at the end in a fixed order, which halves the
+// dependency chain; where both rows are 16-byte aligned, 16-byte loads of two
+// coordinates, four in flight, so that the loads of a long row overlap
+// instead of waiting one after another.
 __device__ __forceinline__ void ff_dist2(const float2 *__restrict__ x, const float2 *__restrict__ y, int k,
                                          float &th, float &tl)
 {
-  float sh = 0.f, sl = 0.f;
-  for (int p = 0; p < k; p++) {
-    const float2 u = x[p], v = y[p];
-    const float s = u.x - v.x;                       // TwoSum(u.x, -v.x)
-    const float bv = s - u.x;
-    float e = (u.x - (s - bv)) + (-v.x - bv);
-    e += u.y - v.y;
-    const float dh = s + e, dl = e - (dh - s);       // Fast2Sum
-    const float q = dh * dh;
-    const float qe = fmaf(dh, dh, -q) + 2.f * dh * dl;
-    const float t = sh + q;                          // TwoSum(sh, q)
-    const float z = t - sh;
-    sl += ((sh - (t - z)) + (q - z)) + qe;
-    sh = t;
+  float sh0 = 0.f, sl0 = 0.f, sh1 = 0.f, sl1 = 0.f;
+  int p = 0;
+  if (((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(y)) & 15) == 0) {
+    const float4 *__restrict__ x4 = reinterpret_cast<const float4 *>(x);
+    const float4 *__restrict__ y4 = reinterpret_cast<const float4 *>(y);
+    const int k2 = k >> 1;
+#pragma unroll 4
+    for (int q = 0; q < k2; q++) {
+      const float4 a = __ldg(x4 + q), b = __ldg(y4 + q);
+      ff_acc(make_float2(a.x, a.y), make_float2(b.x, b.y), sh0, sl0);
+      ff_acc(make_float2(a.z, a.w), make_float2(b.z, b.w), sh1, sl1);
+    }
+    p = k2 << 1;
   }
-  th = sh + sl;
-  tl = sl - (th - sh);
+  for (; p < k; p++) ff_acc(x[p], y[p], sh0, sl0);
+  // (sh0 + sl0) + (sh1 + sl1): TwoSum of the high parts, then the low parts
+  const float t = sh0 + sh1;
+  const float z = t - sh0;
+  const float e = ((sh0 - (t - z)) + (sh1 - z)) + (sl0 + sl1);
+  th = t + e;
+  tl = e - (th - t);
 }
 
 // Recheck of one pair.  The list form keeps float-pair copies of the pools:
@@ -1135,11 +1161,53 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
   return recheck64<KT>(a, T.kp, pa, pb, jpos);
 }
 
+// ff_dist2 by a whole warp for one pair (every lane passes the same rows):
+// lane l takes coordinates l, l + 32, ... (coalesced loads, two accumulators),
+// then a butterfly of TwoSums adds the lanes' double-float partials.  TwoSum
+// is exact whichever operand comes first, so every lane ends with the same
+// float pair; the order is fixed (deterministic).
+__device__ __forceinline__ void ff_dist2_warp(const float2 *__restrict__ x, const float2 *__restrict__ y, int k,
+                                              float &th, float &tl)
+{
+  const int lane = threadIdx.x & 31;
+  float sh0 = 0.f, sl0 = 0.f, sh1 = 0.f, sl1 = 0.f;
+  int p = lane;
+#pragma unroll 2
+  for (; p + 32 < k; p += 64) {
+    const float2 u0 = __ldg(x + p), v0 = __ldg(y + p), u1 = __ldg(x + p + 32), v1 = __ldg(y + p + 32);
+    ff_acc(u0, v0, sh0, sl0);
+    ff_acc(u1, v1, sh1, sl1);
+  }
+  if (p < k) ff_acc(__ldg(x + p), __ldg(y + p), sh0, sl0);
+  float h, l;
+  {
+    const float t = sh0 + sh1, z = t - sh0;
+    const float e = ((sh0 - (t - z)) + (sh1 - z)) + (sl0 + sl1);
+    h = t + e;
+    l = e - (h - t);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, h, o), l2 = __shfl_xor_sync(0xffffffffu, l, o);
+    const float t = h + h2, z = t - h;
+    const float e = ((h - (t - z)) + (h2 - z)) + (l + l2);
+    h = t + e;
+    l = e - (h - t);
+  }
+  th = h;
+  tl = l;
+}
+
+// Rows of at least this many coordinates are rechecked by a whole warp per
+// pair (ff_dist2_warp), shorter ones by one lane per pair (ff_dist2).
+constexpr int WARP_RECHECK_K = 256;
+
 // A flagged pair of the Gaussian kinds, FP64-free: the flag rules select pairs
 // whose value lies in the FP32 range, so the value (float-pair distance from
 // the pools' float-pair copies, then exp2_prod) times the column's FP32 weight
 // is formed in FP32 like the main path's.  Needs the copies (ffp).
-template <int KT>
+// WARP: called by the whole warp for the same pair (ff_dist2_warp).
+template <int KT, bool WARP = false>
 __device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T, int ipos, float ah, float ahl,
                                            const SrcMeta *__restrict__ bm, int c)
 {
@@ -1149,7 +1217,9 @@ __device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T
   if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
   if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
   float th, tl;
-  ff_dist2(a.XAf + (size_t)(a.ffpos ? ipos : pa) * a.k, a.XBf + (size_t)(a.ffpos ? jpos : pb) * a.k, a.k, th, tl);
+  const float2 *x = a.XAf + (size_t)(a.ffpos ? ipos : pa) * a.k, *y = a.XBf + (size_t)(a.ffpos ? jpos : pb) * a.k;
+  if constexpr (WARP) ff_dist2_warp(x, y, a.k, th, tl);
+  else ff_dist2(x, y, a.k, th, tl);
   float ph, pl;
   if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
     // (-0.5 log2e hi) hj from the row's and the column's float pairs
@@ -1165,9 +1235,12 @@ __device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T
 
 // The flagged pairs of one warp's 32 rows (lanes) x 32 columns, all lanes
 // working: the flags are numbered lane by lane (fl: this lane's columns, bit
-// j = column 32 grp + j), 32 per round; each lane rechecks one (recheck_f),
-// and each row adds its own values in their order (through the warp's
-// 32-float scratch wq) to add, their magnitudes to fchk.
+// j = column 32 grp + j), 32 per round; each lane finds one, and either
+// rechecks it (recheck_f, short rows) or the warp rechecks the round's pairs
+// one after another with its lanes over the coordinates (long rows: coalesced
+// loads instead of 32 rows read side by side).  Each row adds its own values
+// in their order (through the warp's 32-float scratch wq) to add, their
+// magnitudes to fchk.
 template <int KT>
 __device__ __forceinline__ void recheck_warp(const TileArgs &a, const TaskParam &T, const PtMeta &am,
                                              const SrcMeta *__restrict__ bm, int grp, uint32_t fl,
@@ -1184,6 +1257,7 @@ __device__ __forceinline__ void recheck_warp(const TileArgs &a, const TaskParam 
   }
   const int excl = incl - cnt;
   const int tot = __shfl_sync(full, incl, 31);
+  if (lane == 0 && a.nrecheck) atomicAdd(a.nrecheck, (unsigned long long)tot);
   for (int base = 0; base < tot; base += 32) {
     const int e = base + lane;
     int L = 0;                       // the owner: lanes before it have incl <= e
@@ -1199,10 +1273,25 @@ __device__ __forceinline__ void recheck_warp(const TileArgs &a, const TaskParam 
     const float hL = __shfl_sync(full, am.h, L);
     const float hlL = __shfl_sync(full, __int_as_float(am.pad[1]), L);
     float v = 0.f;
+    int col = -1;
     if (e < tot) {
       uint32_t mk = flL;             // its (e - exL)-th flagged column
       for (int i = e - exL; i > 0 && mk; i--) mk &= mk - 1;
-      if (mk) v = recheck_f<KT>(a, T, posL, hL, hlL, bm, grp * 32 + __ffs(mk) - 1);
+      if (mk) col = grp * 32 + __ffs(mk) - 1;
+    }
+    if (a.k >= WARP_RECHECK_K) {
+      const int ne = min(32, tot - base);
+      for (int q = 0; q < ne; q++) {
+        const int cq = __shfl_sync(full, col, q);
+        const int pq = __shfl_sync(full, posL, q);
+        const float hq = __shfl_sync(full, hL, q), hlq = __shfl_sync(full, hlL, q);
+        if (cq >= 0) {
+          const float r = recheck_f<KT, true>(a, T, pq, hq, hlq, bm, cq);
+          if (lane == q) v = r;
+        }
+      }
+    } else if (col >= 0) {
+      v = recheck_f<KT>(a, T, posL, hL, hlL, bm, col);
     }
     wq[lane] = v;
     __syncwarp();
@@ -1533,6 +1622,7 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
         const int c = c0 + j;
         if (c < ncols && am.pos >= 0) {
           const double v = recheck<KT>(a, T, ltab, am.pos, bm->pos[c]);
+          if (a.nrecheck) atomicAdd(a.nrecheck, 1ull);
           rchk += v;
           fchk += fabsf((float)v);
           nchk = true;
@@ -2103,7 +2193,14 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   a.stall = tl_split_stall;
   const int grid = std::min(ntm * nsc, sms);
   int *rlist = defer ? (int *)(ws + o_rl) : nullptr, *rcount = defer ? (int *)(ws + o_rc) : nullptr;
-  cudaError_t e = cudaMemsetAsync(a.next_item, 0, sizeof(int), s);
+  // diagnostics of this call (gsks_split_stats): rechecked pairs, rescued rows
+  if (!c->stats.ensure(16)) {
+    if (stream_ordered_alloc) cudaFreeAsync(ws, s);
+    return GSKS_ERR_ALLOC;
+  }
+  a.nrecheck = (unsigned long long *)c->stats.p;
+  cudaError_t e = cudaMemsetAsync(c->stats.p, 0, 16, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.next_item, 0, sizeof(int), s);
   if (e == cudaSuccess && defer) e = cudaMemsetAsync(rcount, 0, sizeof(int), s);
   if (e == cudaSuccess) e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
   if (e == cudaSuccess) {
@@ -2111,6 +2208,8 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
                                                  anch ? ybar + k : nullptr);
     e = cudaGetLastError();
   }
+  if (e == cudaSuccess && defer)
+    e = cudaMemcpyAsync((uint8_t *)c->stats.p + 8, rcount, sizeof(int), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess && defer) e = launch_rescue(a, std::max(1, std::min(2 * sms, (m + 7) / 8)), rlist, rcount, u, umap, s);
   if (stream_ordered_alloc) cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_status(e, "split launch");
@@ -2434,6 +2533,22 @@ int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int 
 }  // namespace gsks
 
 using namespace gsks;
+
+// Diagnostics (gsks.h) of this thread's last single split-precision call.
+extern "C" int gsks_split_stats(long long *rechecked_pairs, int *rescued_rows)
+{
+  Ctx *c = get_ctx();
+  if (!c) return gsks_last_error();
+  unsigned long long v[2] = {0, 0};
+  if (c->stats.p) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(v, c->stats.p, 16, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e, "gsks_split_stats");
+  }
+  if (rechecked_pairs) *rechecked_pairs = (long long)v[0];
+  if (rescued_rows) *rescued_rows = (int)(v[1] & 0xffffffffu);
+  return set_status(GSKS_OK, nullptr);
+}
 
 // Test hook (gsks.h): the wait limit and the producer stall of this thread's
 // later split-precision calls.

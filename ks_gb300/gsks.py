@@ -91,6 +91,8 @@ def load():
     lib.gsks_list_plan_errors.argtypes = [vp]
     lib.gsks_list_plan_destroy.restype = C.c_int
     lib.gsks_list_plan_destroy.argtypes = [vp]
+    lib.gsks_split_stats.restype = C.c_int
+    lib.gsks_split_stats.argtypes = [C.POINTER(C.c_longlong), C.POINTER(C.c_int)]
     lib.gsks_split_test_wait.restype = C.c_int
     lib.gsks_split_test_wait.argtypes = [C.c_longlong, C.c_int]
     _lib = lib
@@ -112,6 +114,16 @@ def last_launch_count() -> int:
 def device_errors() -> int:
     """Device-side error flags of this thread's context (read and cleared)."""
     return int(load().gsks_device_errors())
+
+
+def split_stats() -> dict:
+    """Rechecked pairs and rescued rows of this thread's last single
+    split-precision call (waits for the device)."""
+    r, q = C.c_longlong(), C.c_int()
+    rc = load().gsks_split_stats(C.byref(r), C.byref(q))
+    if rc:
+        raise GsksError(rc, "gsks_split_stats")
+    return {"rechecked_pairs": int(r.value), "rescued_rows": int(q.value)}
 
 
 def split_test_wait(wait_cycles: int = 0, stall: bool = False) -> None:
