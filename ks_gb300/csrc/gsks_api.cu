@@ -325,11 +325,10 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
                   const double *w, const int *wmap, const double *hi, const double *hj,
                   int precision, cudaStream_t s, bool stream_ordered_alloc, int nrhs)
 {
-  // nrhs > 1: FP64 form only (interleaved u and w, each K formed once)
-  if (nrhs > 1 && precision != GSKS_FP64) return GSKS_ERR_ARG;
+  // nrhs > 1: interleaved u and w, each K formed once (up to 4)
   if (precision == GSKS_SPLIT_BF16X3)
     return enqueue_split(c, ker, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb,
-                         w, wmap, hi, hj, s, stream_ordered_alloc);
+                         w, wmap, hi, hj, s, stream_ordered_alloc, std::max(nrhs, 1));
   if (precision != GSKS_FP64) return GSKS_ERR_PRECISION;
 
   Fp64Plan p = fp64_plan(m, n, k, c->num_sms);
@@ -364,9 +363,10 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
 
 // ---- several right-hand sides -------------------------------------------
 // u and w hold nrhs interleaved columns, as the reference lays them out for
-// KS_RHS > 1 (u[umap[i] * KS_RHS + r], w[wmap[j] * KS_RHS + r]).  The FP64
-// form takes up to four in one pass, each kernel value multiplied by every
-// weight column.  Otherwise right-hand side r is one evaluation with the maps
+// KS_RHS > 1 (u[umap[i] * KS_RHS + r], w[wmap[j] * KS_RHS + r]).  Both forms
+// take up to four in one pass, each kernel value multiplied by every weight
+// column.  Otherwise (more than four, or a split layout without room for the
+// extra weights) right-hand side r is one evaluation with the maps
 // umap[i] * nrhs + r and wmap[j] * nrhs + r, built on the device, and the
 // kernel values are evaluated again for every r.
 __global__ void rhs_map_kernel(int cnt, const int *__restrict__ map, int nrhs, int r, int *__restrict__ out)
@@ -381,9 +381,13 @@ int enqueue_rhs(Ctx *c, const ks_t *ker, int m, int n, int k, int nrhs, double *
                 const double *w, const int *wmap, const double *hi, const double *hj,
                 int precision, cudaStream_t s, bool stream_ordered_alloc)
 {
-  if (nrhs == 1 || (precision == GSKS_FP64 && nrhs <= 4))   // one pass, each K formed once
-    return enqueue_fused(c, ker, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb, w, wmap, hi, hj,
-                         precision, s, stream_ordered_alloc, nrhs);
+  if (nrhs <= 4) {   // one pass, each K formed once
+    const int st = enqueue_fused(c, ker, m, n, k, u, umap, XA, XA2, amap, nxa, XB, XB2, bmap, nxb, w, wmap, hi, hj,
+                                 precision, s, stream_ordered_alloc, nrhs);
+    // the split form's sweep of several columns needs more shared memory than
+    // some layouts leave (the Laplace table beyond k = 64): one sweep per column
+    if (!(st == GSKS_ERR_TOO_LARGE && precision == GSKS_SPLIT_BF16X3 && nrhs > 1 && k <= 1024)) return st;
+  }
   const size_t bytes = ((size_t)m + n) * sizeof(int);
   int *maps = nullptr;
   if (stream_ordered_alloc) {

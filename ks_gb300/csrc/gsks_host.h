@@ -86,13 +86,15 @@ int enqueue_fused(Ctx *c, const ks_t *ker, int m, int n, int k,
                   const double *w, const int *wmap, const double *hi, const double *hj,
                   int precision, cudaStream_t s, bool stream_ordered_alloc, int nrhs = 1);
 
-// Split-precision form (gsks_split.cu).
+// Split-precision form (gsks_split.cu).  nrhs <= 4 interleaved columns of u
+// and w in one sweep; GSKS_ERR_TOO_LARGE when k or the shared memory of that
+// sweep does not fit (the caller then sweeps once per column).
 int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k,
                   double *u, const int *umap,
                   const double *XA, const double *XA2, const int *amap, int nxa,
                   const double *XB, const double *XB2, const int *bmap, int nxb,
                   const double *w, const int *wmap, const double *hi, const double *hj,
-                  cudaStream_t s, bool stream_ordered_alloc);
+                  cudaStream_t s, bool stream_ordered_alloc, int nrhs = 1);
 
 // Split-precision form of dgsks_list (gsks_split.cu), planned once for a set
 // of lists: row sums of every (task t, target position r, source chunk sc)

@@ -96,6 +96,24 @@ struct SrcMeta {
 };
 static_assert(sizeof(SrcMeta) == BN * sizeof(PtMeta), "both metadata blocks take 32 bytes per point");
 
+// Several right-hand sides in one sweep: up to RMAX weight columns per source,
+// each kernel value multiplied by all of them.  Source tiles then carry 48
+// bytes of metadata per point: the 32 of SrcMeta (w = column 0, wsum = the
+// sum over columns of |w|), then the other columns' weights and a pad.
+constexpr int RMAX = 4;
+struct SrcMetaX {
+  SrcMeta m;
+  float wx[RMAX - 1][BN];
+  float pad2[BN];
+};
+static_assert(sizeof(SrcMetaX) == BN * 48, "48 bytes per point with several right-hand sides");
+__host__ __device__ constexpr size_t smeta_pt(int nr) { return nr > 1 ? 48 : 32; }
+// Weights of column r of a source tile's metadata.
+__device__ __forceinline__ const float *wrow(const SrcMeta *bm, int r)
+{
+  return r == 0 ? bm->w : reinterpret_cast<const SrcMetaX *>(bm)->wx[r - 1];
+}
+
 __device__ __forceinline__ float4 ld4(const float *p) { return *(const float4 *)p; }
 __device__ __forceinline__ float f4(const float4 &v, int i) { return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w; }
 
@@ -180,9 +198,10 @@ struct SplitTaskGeo {
 };
 
 __host__ __device__ inline size_t blk_bytes(int rows, int kpad) { return (size_t)rows * kpad * 2; }
-__host__ __device__ inline size_t tile_bytes(int rows, int kpad)
+// mpt: metadata bytes per point (32; 48 for source tiles of several right-hand sides)
+__host__ __device__ inline size_t tile_bytes(int rows, int kpad, size_t mpt = sizeof(PtMeta))
 {
-  return NBLK * blk_bytes(rows, kpad) + (size_t)rows * sizeof(PtMeta);
+  return NBLK * blk_bytes(rows, kpad) + (size_t)rows * mpt;
 }
 
 // k is processed in chunks of KCH (the whole padded k when it is smaller);
@@ -210,6 +229,7 @@ struct SmemLayout {
   size_t chunk_al;     // chunk_op rounded up to 1 KiB
   size_t stage_bytes;  // one stage: the source chunk, or both operands' chunks
   size_t a_region;     // target image (resident) or target metadata
+  size_t smeta;        // one source-metadata slot (BN points)
   int tab_sh;          // Laplace table: log2 of its copies (0 or 3), -1 without table
 };
 __host__ __device__ inline size_t smem_fixed(const SmemLayout &L);
@@ -219,9 +239,11 @@ __host__ __device__ inline size_t smem_fixed(const SmemLayout &L);
 // a quarter warp, so that table lookups never conflict; the resident Laplace
 // form then keeps two source stages instead of three (its epilogue, not the
 // copies, sets the pace).
-__host__ __device__ inline SmemLayout smem_layout(int kpad, int kt)
+// nr: right-hand sides of the sweep (1, or RMAX: larger source metadata).
+__host__ __device__ inline SmemLayout smem_layout(int kpad, int kt, int nr = 1)
 {
   SmemLayout L;
+  L.smeta = (size_t)BN * smeta_pt(nr);
   L.kc = kchunk(kpad);
   L.nch = kpad / L.kc;
   L.resident = (L.nch == 1);
@@ -546,9 +568,10 @@ constexpr int ANCHOR_WPER = 4096;   // weights per block of the weight sum
 __global__ void __launch_bounds__(256) anchor_partial(int n, int k, const double *__restrict__ XB,
                                                       const int *__restrict__ bmap, int nxb,
                                                       const double *__restrict__ w, const int *__restrict__ wmap,
-                                                      int *err, double *__restrict__ ybar,
+                                                      int nrhs, int *err, double *__restrict__ ybar,
                                                       double *__restrict__ wpart)
 {
+  // nrhs interleaved weight columns: one sum per column (wpart[b nrhs + r])
   __shared__ double sh[256];
   const int ncb = (k + 31) / 32, t = threadIdx.x, lane = t & 31, wp = t >> 5;
   if ((int)blockIdx.x < ncb) {
@@ -570,23 +593,27 @@ __global__ void __launch_bounds__(256) anchor_partial(int n, int k, const double
   }
   const int b = blockIdx.x - ncb;
   const int j0 = b * ANCHOR_WPER, j1 = min(n, j0 + ANCHOR_WPER);
-  double s = 0.0;
-  for (int j = j0 + t; j < j1; j += 256) s += w[wmap ? wmap[j] : j];
-  sh[t] = s;
-  __syncthreads();
-  for (int h = 128; h > 0; h >>= 1) {
-    if (t < h) sh[t] += sh[t + h];
+  for (int r = 0; r < nrhs; r++) {
+    double s = 0.0;
+    for (int j = j0 + t; j < j1; j += 256) s += w[(size_t)(wmap ? wmap[j] : j) * nrhs + r];
+    sh[t] = s;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+      if (t < h) sh[t] += sh[t + h];
+      __syncthreads();
+    }
+    if (t == 0) wpart[(size_t)b * nrhs + r] = sh[0];
     __syncthreads();
   }
-  if (t == 0) wpart[b] = sh[0];
 }
 
-__global__ void anchor_final(int nwb, const double *__restrict__ wpart, double *__restrict__ wsum)
+__global__ void anchor_final(int nwb, int nrhs, const double *__restrict__ wpart, double *__restrict__ wsum)
 {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
+  const int r = threadIdx.x;
+  if (blockIdx.x == 0 && r < nrhs) {
     double s = 0.0;
-    for (int b = 0; b < nwb; b++) s += wpart[b];
-    *wsum = s;
+    for (int b = 0; b < nwb; b++) s += wpart[(size_t)b * nrhs + r];
+    wsum[r] = s;
   }
 }
 
@@ -616,8 +643,10 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
                             const double *__restrict__ centre, const Params *__restrict__ P,
                             uint8_t *__restrict__ img, const int2 *__restrict__ tiles,
                             const int *__restrict__ tile_task, const TaskParam *__restrict__ tp,
-                            const double *__restrict__ ybar, double *__restrict__ rowc)
+                            const double *__restrict__ ybar, double *__restrict__ rowc, int nrhs = 1)
 {
+  // nrhs > 1 (sources of several right-hand sides): w holds nrhs interleaved
+  // columns and the tiles carry RMAX weights per point (SrcMetaX)
   const int tile = blockIdx.x, r = threadIdx.x;
   int pt = tile * BM + r;
   bool valid = pt < npts;
@@ -638,7 +667,7 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   const double sc = TT ? TT->sc : P->alpha * P->inv_sigma * 128.0;
   const double sig2 = TT ? TT->sig2 : P->sigma * P->sigma;
   const bool gfast = TT ? TT->gfast != 0 : P->gfast != 0;
-  uint8_t *base = img + (size_t)tile * tile_bytes(BM, kpad);
+  uint8_t *base = img + (size_t)tile * tile_bytes(BM, kpad, side == 1 ? smeta_pt(nrhs > 1 ? RMAX : 1) : sizeof(PtMeta));
   const size_t bb = blk_bytes(BM, kpad);
   // The norm of the represented point restricted to the products the tensor
   // cores form (a1a1 + 2a1a2 + a2a2 + 2a1a3), so that the assembled d2 of
@@ -690,13 +719,15 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   mt.n_lo = (float)nl;
   mt.w = 0.0f;
   mt.h = 0.0f;
-  if (side == 1 && valid) mt.w = (float)w[wmap ? wmap[pt] : pt];
+  const size_t wi = valid ? (size_t)(wmap ? wmap[pt] : pt) * (nrhs > 1 ? nrhs : 1) : 0;   // weight column 0
+  double wf = 1.0;                 // the Gaussian fast path's source factor
+  if (side == 1 && valid) mt.w = (float)w[wi];
   if (gfast) {
     // Gaussian: 2^-(g nl) is a per-point factor; fold it into w for sources
     // and into a row factor for targets (applied to the row sum)
     const double f = exp2(-g * nl);
     mt.n_lo = 0.0f;
-    if (side == 1) mt.w = valid ? (float)(w[wmap ? wmap[pt] : pt] * f) : 0.0f;
+    if (side == 1) { mt.w = valid ? (float)(w[wi] * f) : 0.0f; wf = f; }
     else mt.h = (float)f;
   }
   mt.pos = valid ? pt : -1;
@@ -741,12 +772,22 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
     ((PtMeta *)(base + NBLK * bb))[r] = mt;
     return;
   }
-  // sources: sum of |w| over each group of 32 columns, kept with the group's
-  // first column (the underflow test of the exponential kernels)
+  // sources: sum of |w| (over the weight columns) over each group of 32
+  // columns, kept with the group's first column (the underflow test of the
+  // exponential kernels)
   float wa = fabsf(mt.w);
+  SrcMeta *sm = (SrcMeta *)(base + NBLK * bb);
+  if (nrhs > 1) {
+    SrcMetaX *sx = (SrcMetaX *)sm;
+    for (int c = 1; c < RMAX; c++) {
+      const float wc = (valid && c < nrhs) ? (float)(w[wi + c] * wf) : 0.0f;
+      sx->wx[c - 1][r] = wc;
+      wa += fabsf(wc);
+    }
+    sx->pad2[r] = 0.0f;
+  }
 #pragma unroll
   for (int o = 16; o; o >>= 1) wa += __shfl_xor_sync(0xffffffffu, wa, o);
-  SrcMeta *sm = (SrcMeta *)(base + NBLK * bb);
   sm->n_hi[r] = mt.n_hi; sm->n_lo[r] = mt.n_lo; sm->w[r] = mt.w; sm->h[r] = mt.h;
   sm->pos[r] = mt.pos;
   sm->wsum[r] = (r & 31) == 0 ? wa : 0.0f;
@@ -763,6 +804,7 @@ struct TileArgs {
   const float2 *XAf, *XBf;          // float-pair copies for the rechecks (or nullptr)
   int ffpos;                        // the copies are indexed by position (else by pool point)
   unsigned long long *nrecheck;     // count of rechecked pairs (or nullptr)
+  int nrhs;                         // interleaved columns of u and w (the FP64 weights of the rechecks)
   const int *amap, *bmap, *wmap;
   int nxa, nxb;                     // pool sizes for the map range checks (-1: unchecked)
   const double *w;
@@ -828,8 +870,8 @@ struct SplitSmem {
 // Shared memory without the Laplace table (which follows SplitSmem).
 __host__ __device__ inline size_t smem_fixed(const SmemLayout &L)
 {
-  return 1024 /* alignment slack */ + L.a_region + L.nstage * L.stage_bytes + NMETA * (size_t)BN * sizeof(PtMeta) +
-         sizeof(SplitSmem) + 64;
+  return 1024 /* alignment slack */ + L.a_region + L.nstage * L.stage_bytes + NMETA * L.smeta + sizeof(SplitSmem) +
+         64;
 }
 
 // The largest non-table layout (resident k = KPAD_MAX, NSTAGE source stages)
@@ -1035,14 +1077,13 @@ __device__ __forceinline__ float kval32(float t, float lo, float c, float hrow, 
 }
 
 // FP64 recheck of one flagged pair from the pool coordinates (the distance
-// assembly of near-coincident pairs is kept in FP64).
+// assembly of near-coincident pairs is kept in FP64): the kernel value.
 template <int KT>
-__device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb, int jpos)
+__device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb)
 {
   const double *x = a.XA + (size_t)pa * a.k, *y = a.XB + (size_t)pb * a.k;
   double d2 = 0.0;
   for (int p = 0; p < a.k; p++) { const double d = x[p] - y[p]; d2 = fma(d, d, d2); }
-  const double wv = a.w[a.wmap ? a.wmap[jpos] : jpos];
   double kv;
   if constexpr (KT == KS_GAUSSIAN) kv = exp(d2 * kp.scal);
   else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) kv = exp(((d2 * -0.5) * kp.hi[pa]) * kp.hj[pb]);
@@ -1054,7 +1095,13 @@ __device__ double recheck64(const TileArgs &a, const KParams &kp, int pa, int pb
   } else if constexpr (KT == KS_MULTIQUADRATIC) kv = d2 + kp.cons;
   else if constexpr (KT == KS_EPANECHNIKOV) kv = d2 < 1.0 ? 0.75 * (1.0 - d2) : 0.0;
   else kv = 0.0;
-  return kv * wv;
+  return kv;
+}
+
+// Weight r (of a.nrhs interleaved columns) of source position jpos, in FP64.
+__device__ __forceinline__ double wcol64(const TileArgs &a, int jpos, int r)
+{
+  return a.w[(size_t)(a.wmap ? a.wmap[jpos] : jpos) * (a.nrhs > 1 ? a.nrhs : 1) + r];
 }
 
 // One coordinate of a float-pair squared distance: (u - v)^2 added to the
@@ -1107,7 +1154,8 @@ __device__ __forceinline__ void ff_dist2(const float2 *__restrict__ x, const flo
   tl = e - (th - t);
 }
 
-// Recheck of one pair.  The list form keeps float-pair copies of the pools:
+// Recheck of one pair: its kernel value (the caller applies the weights).
+// The list form keeps float-pair copies of the pools:
 // there the squared distance is summed in float-pair arithmetic (TwoSum per
 // coordinate difference, exact square by FMA; about 2^-44 relative) and the
 // kernel value is formed in FP32 from it, as in the main epilogue; FP64
@@ -1138,27 +1186,26 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
       }
       float th, tl;
       ff_dist2(x, y, a.k, th, tl);
-      const double wv = a.w[a.wmap ? a.wmap[jpos] : jpos];
       bool deep = false;
       if constexpr (KT == KS_GAUSSIAN) {
-        const double v = exp2_prod_wide(th, tl, T.s2, T.s2l, deep) * wv;
+        const double v = exp2_prod_wide(th, tl, T.s2, T.s2l, deep);
         if (!deep) return v;
       } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
         const double f = -0.5 * 1.4426950408889634 * hf;
         const float fh = (float)f, fl = (float)(f - (double)fh);
-        const double v = exp2_prod_wide(th, tl, fh, fl, deep) * wv;
+        const double v = exp2_prod_wide(th, tl, fh, fl, deep);
         if (!deep) return v;
       } else {
         if (th > T.lap.tover && th >= 1e-15f) {
           int n;
           const float y = laplace_core(th, tl, ltab, T.lap, n);
-          if (n >= -1020) return scale2(y, n) * wv;
+          if (n >= -1020) return scale2(y, n);
           if (n <= -1090) return 0.0;
         }
       }
     }
   }
-  return recheck64<KT>(a, T.kp, pa, pb, jpos);
+  return recheck64<KT>(a, T.kp, pa, pb);
 }
 
 // ff_dist2 by a whole warp for one pair (every lane passes the same rows):
@@ -1230,7 +1277,7 @@ __device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T
     ph = T.s2;
     pl = T.s2l;
   }
-  return exp2_prod(th, tl, ph, pl) * bm->w[c];
+  return exp2_prod(th, tl, ph, pl);   // the caller applies the column's weights
 }
 
 // The flagged pairs of one warp's 32 rows (lanes) x 32 columns, all lanes
@@ -1241,10 +1288,10 @@ __device__ __forceinline__ float recheck_f(const TileArgs &a, const TaskParam &T
 // loads instead of 32 rows read side by side).  Each row adds its own values
 // in their order (through the warp's 32-float scratch wq) to add, their
 // magnitudes to fchk.
-template <int KT>
+template <int KT, int NR>
 __device__ __forceinline__ void recheck_warp(const TileArgs &a, const TaskParam &T, const PtMeta &am,
                                              const SrcMeta *__restrict__ bm, int grp, uint32_t fl,
-                                             float *wq, float &add, float &fchk)
+                                             float *wq, float (&add)[NR], float &fchk)
 {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -1272,7 +1319,7 @@ __device__ __forceinline__ void recheck_warp(const TileArgs &a, const TaskParam 
     const int posL = __shfl_sync(full, am.pos, L);
     const float hL = __shfl_sync(full, am.h, L);
     const float hlL = __shfl_sync(full, __int_as_float(am.pad[1]), L);
-    float v = 0.f;
+    float kv = 0.f;
     int col = -1;
     if (e < tot) {
       uint32_t mk = flL;             // its (e - exL)-th flagged column
@@ -1287,21 +1334,24 @@ __device__ __forceinline__ void recheck_warp(const TileArgs &a, const TaskParam 
         const float hq = __shfl_sync(full, hL, q), hlq = __shfl_sync(full, hlL, q);
         if (cq >= 0) {
           const float r = recheck_f<KT, true>(a, T, pq, hq, hlq, bm, cq);
-          if (lane == q) v = r;
+          if (lane == q) kv = r;
         }
       }
     } else if (col >= 0) {
-      v = recheck_f<KT>(a, T, posL, hL, hlL, bm, col);
+      kv = recheck_f<KT>(a, T, posL, hL, hlL, bm, col);
     }
-    wq[lane] = v;
-    __syncwarp();
     const int q1 = min(incl, base + 32) - base;
-    for (int q = max(excl, base) - base; q < q1; q++) {
-      const float x = wq[q];
-      add += x;
-      fchk += fabsf(x);
+#pragma unroll
+    for (int r = 0; r < NR; r++) {   // each weight column: the values through wq, rows in order
+      wq[lane] = col >= 0 ? kv * wrow(bm, r)[col] : 0.f;
+      __syncwarp();
+      for (int q = max(excl, base) - base; q < q1; q++) {
+        const float x = wq[q];
+        add[r] += x;
+        fchk += fabsf(x);
+      }
+      __syncwarp();
     }
-    __syncwarp();
   }
 }
 
@@ -1356,19 +1406,25 @@ __device__ __forceinline__ void assemble2(uint64_t H, uint64_t L, uint64_t AN, u
 }
 
 // NC columns of one row, Gaussian with the low norm parts folded into the
-// source weights and the row factor: kv = 2^-(g tt) (1 - ln2 g ee).
-template <int NC>
+// source weights and the row factor: kv = 2^-(g tt) (1 - ln2 g ee), times
+// the NR weight columns (acc[r]).
+template <int NC, int NR>
 __device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                                 const SrcMeta *__restrict__ bm, int c0, float an_hi, float rc,
-                                                float (&acc)[4])
+                                                float (&acc)[NR][4])
 {
-  // two columns per instruction (packed FP32 pairs); column j feeds acc[j & 3]
+  // two columns per instruction (packed FP32 pairs); column j feeds acc[.][j & 3]
   const float cg = 0.69314718f * rc;          // -ln2 g
   const uint64_t AN = pk2(an_hi, an_hi), RC = pk2(rc, rc), CG = pk2(cg, cg);
-  uint64_t A01 = pk2(acc[0], acc[1]), A23 = pk2(acc[2], acc[3]);
+  uint64_t A01[NR], A23[NR];
+#pragma unroll
+  for (int r = 0; r < NR; r++) { A01[r] = pk2(acc[r][0], acc[r][1]); A23[r] = pk2(acc[r][2], acc[r][3]); }
 #pragma unroll
   for (int j4 = 0; j4 < NC; j4 += 4) {
-    const float4 nh = ld4(&bm->n_hi[c0 + j4]), ww = ld4(&bm->w[c0 + j4]);   // nu_hi, w'
+    const float4 nh = ld4(&bm->n_hi[c0 + j4]);                              // nu_hi
+    float4 ww[NR];                                                          // w' of each column
+#pragma unroll
+    for (int r = 0; r < NR; r++) ww[r] = ld4(wrow(bm, r) + c0 + j4);
 #pragma unroll
     for (int q = 0; q < 4; q += 2) {
       const int j = j4 + q;
@@ -1380,20 +1436,27 @@ __device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const u
       const uint64_t ar = mul2(tt, RC);
       const uint64_t E = pk2(ex2_approx(lo2(ar)), ex2_approx(hi2(ar)));       // 2^-(g tt)
       const uint64_t kv = fma2(E, mul2(CG, ee), E);
-      const uint64_t W = pk2(f4(ww, q), f4(ww, q + 1));
-      if (q == 0) A01 = fma2(kv, W, A01);
-      else A23 = fma2(kv, W, A23);
+#pragma unroll
+      for (int r = 0; r < NR; r++) {
+        const uint64_t W = pk2(f4(ww[r], q), f4(ww[r], q + 1));
+        if (q == 0) A01[r] = fma2(kv, W, A01[r]);
+        else A23[r] = fma2(kv, W, A23[r]);
+      }
     }
   }
-  acc[0] = lo2(A01); acc[1] = hi2(A01); acc[2] = lo2(A23); acc[3] = hi2(A23);
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    acc[r][0] = lo2(A01[r]); acc[r][1] = hi2(A01[r]); acc[r][2] = lo2(A23[r]); acc[r][3] = hi2(A23[r]);
+  }
 }
 
-// NC columns of one row, distance kernels.  Returns the flagged columns.
-template <int KT, bool EXACT, bool FLAGS, int NC>
+// NC columns of one row, distance kernels, NR weight columns.  Returns the
+// flagged columns.
+template <int KT, bool EXACT, bool FLAGS, int NC, int NR>
 __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                               const SrcMeta *__restrict__ bm, int c0, const PtMeta &am, float rc,
                                               const TaskParam &T, const LTab &ltab,
-                                              float (&acc)[4], float &amin)
+                                              float (&acc)[NR][4], float &amin)
 {
   const KParams &kp = T.kp;
   uint32_t flags = 0;
@@ -1403,7 +1466,9 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
 #pragma unroll
   for (int j4 = 0; j4 < NC; j4 += 4) {
     const float4 nh = ld4(&bm->n_hi[c0 + j4]), nl = ld4(&bm->n_lo[c0 + j4]);
-    const float4 ww = ld4(&bm->w[c0 + j4]);
+    float4 ww[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) ww[r] = ld4(wrow(bm, r) + c0 + j4);
     float4 hh = make_float4(0.f, 0.f, 0.f, 0.f), hl = hh;
     if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) { hh = ld4(&bm->h[c0 + j4]); hl = ld4(&bm->hlo[c0 + j4]); }
     uint64_t T2[2], LO2[2], S2[2];
@@ -1453,7 +1518,8 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
         }
       }
       // padding columns carry w = 0 and finite distances
-      acc[q] = fmaf(kv, f4(ww, q), acc[q]);
+#pragma unroll
+      for (int r = 0; r < NR; r++) acc[r][q] = fmaf(kv, f4(ww[r], q), acc[r][q]);
     }
   }
   return flags;
@@ -1462,20 +1528,24 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
 // NC columns of one row, inner-product kernels (polynomial, tanh).  PW in
 // 1..4: a polynomial of that integer power, multiplied out; its values are
 // finite on padding columns (x.y = 0 there), whose weight 0 then needs no mask.
-template <int KT, int NC, int PW = 0>
+template <int KT, int NC, int NR, int PW = 0>
 __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                              const SrcMeta *__restrict__ bm, int c0, int valid, float rc,
-                                             const KParams &kp, float (&acc)[4])
+                                             const KParams &kp, float (&acc)[NR][4])
 {
   // two columns per instruction where the kernel allows it (packed FP32 pairs)
   const uint64_t RC = pk2(rc, rc), MH = pk2(-0.5f, -0.5f);
   const float sc = kp.fscal, cn = kp.fcons;
   const uint64_t SC = pk2(sc, sc), CN = pk2(cn, cn);
   const bool ipow = KT == KS_POLYNOMIAL && kp.pmode == POW_INT;
-  uint64_t A[2] = {pk2(acc[0], acc[1]), pk2(acc[2], acc[3])};
+  uint64_t A[NR][2];
+#pragma unroll
+  for (int r = 0; r < NR; r++) { A[r][0] = pk2(acc[r][0], acc[r][1]); A[r][1] = pk2(acc[r][2], acc[r][3]); }
 #pragma unroll
   for (int j4 = 0; j4 < NC; j4 += 4) {
-    const float4 ww = ld4(&bm->w[c0 + j4]);
+    float4 ww[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) ww[r] = ld4(wrow(bm, r) + c0 + j4);
 #pragma unroll
     for (int p2 = 0; p2 < 2; p2++) {
       const int j = j4 + 2 * p2;
@@ -1488,7 +1558,9 @@ __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint
         if constexpr (PW == 2) R = mul2(V, V);
         if constexpr (PW == 3) R = mul2(mul2(V, V), V);
         if constexpr (PW == 4) { R = mul2(V, V); R = mul2(R, R); }
-        A[p2] = fma2(R, pk2(f4(ww, 2 * p2), f4(ww, 2 * p2 + 1)), A[p2]);
+#pragma unroll
+        for (int r = 0; r < NR; r++)
+          A[r][p2] = fma2(R, pk2(f4(ww[r], 2 * p2), f4(ww[r], 2 * p2 + 1)), A[r][p2]);
         continue;
       }
       float k0, k1;
@@ -1512,10 +1584,15 @@ __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint
       // the kernel of a padding column may be NaN (its weight is 0)
       if (j >= valid) k0 = 0.f;
       if (j + 1 >= valid) k1 = 0.f;
-      A[p2] = fma2(pk2(k0, k1), pk2(f4(ww, 2 * p2), f4(ww, 2 * p2 + 1)), A[p2]);
+#pragma unroll
+      for (int r = 0; r < NR; r++)
+        A[r][p2] = fma2(pk2(k0, k1), pk2(f4(ww[r], 2 * p2), f4(ww[r], 2 * p2 + 1)), A[r][p2]);
     }
   }
-  acc[0] = lo2(A[0]); acc[1] = hi2(A[0]); acc[2] = lo2(A[1]); acc[3] = hi2(A[1]);
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    acc[r][0] = lo2(A[r][0]); acc[r][1] = hi2(A[r][0]); acc[r][2] = lo2(A[r][1]); acc[r][3] = hi2(A[r][1]);
+  }
 }
 
 // NC columns of one row, polynomial of integer power PW in 1..4, summed
@@ -1527,17 +1604,21 @@ __device__ __forceinline__ void epi_chunk_ip(const uint32_t (&h)[NC], const uint
 // variation of K around v0^PW: where K sits on a large constant (v near cons,
 // the sum of K w cancelling), FP32 rounding of K itself would otherwise
 // dominate the error.  Padding columns: finite values, weight 0.
-template <int NC, int PW>
+template <int NC, int PW, int NR>
 __device__ __forceinline__ void epi_chunk_anchor(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                                  const SrcMeta *__restrict__ bm, int c0, const PtMeta &am, float sg,
-                                                 float (&acc)[4])
+                                                 float (&acc)[NR][4])
 {
   const uint64_t H0 = pk2(am.n_hi, am.n_hi), SG = pk2(sg, sg);
   const uint64_t C1 = pk2(am.n_lo, am.n_lo), C2 = pk2(am.w, am.w), C3 = pk2(am.h, am.h);
-  uint64_t A[2] = {pk2(acc[0], acc[1]), pk2(acc[2], acc[3])};
+  uint64_t A[NR][2];
+#pragma unroll
+  for (int r = 0; r < NR; r++) { A[r][0] = pk2(acc[r][0], acc[r][1]); A[r][1] = pk2(acc[r][2], acc[r][3]); }
 #pragma unroll
   for (int j4 = 0; j4 < NC; j4 += 4) {
-    const float4 ww = ld4(&bm->w[c0 + j4]);
+    float4 ww[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) ww[r] = ld4(wrow(bm, r) + c0 + j4);
 #pragma unroll
     for (int p2 = 0; p2 < 2; p2++) {
       const int j = j4 + 2 * p2;
@@ -1549,10 +1630,15 @@ __device__ __forceinline__ void epi_chunk_anchor(const uint32_t (&h)[NC], const 
       else if constexpr (PW == 2) R = mul2(D, add2(D, C1));
       else if constexpr (PW == 3) R = mul2(D, fma2(D, add2(D, C2), C1));
       else R = mul2(D, fma2(D, fma2(D, add2(D, C3), C2), C1));
-      A[p2] = fma2(R, pk2(f4(ww, 2 * p2), f4(ww, 2 * p2 + 1)), A[p2]);
+#pragma unroll
+      for (int r = 0; r < NR; r++)
+        A[r][p2] = fma2(R, pk2(f4(ww[r], 2 * p2), f4(ww[r], 2 * p2 + 1)), A[r][p2]);
     }
   }
-  acc[0] = lo2(A[0]); acc[1] = hi2(A[0]); acc[2] = lo2(A[1]); acc[3] = hi2(A[1]);
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    acc[r][0] = lo2(A[r][0]); acc[r][1] = hi2(A[r][0]); acc[r][2] = lo2(A[r][1]); acc[r][3] = hi2(A[r][1]);
+  }
 }
 
 // Kernels whose FP32 values may fall below the FP32 range while FP64 keeps
@@ -1563,23 +1649,28 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 }
 
 // One warp's share of one tile (32 columns of its 32 rows): TMEM loads, kernel
-// values, weighted sums, FP64 rechecks of the flagged pairs.  Adds the row
-// sum of these columns to racc, and to bsk the columns' sum of |w| where every
-// value of the 32 columns lies below 2^-96.  The 32 columns are summed in FP32 (four
-// interleaved partial sums) and enter the FP64 row sum with one conversion and
-// one add: FP64 instructions issue at a small fraction of the FP32 rate here.
-template <int KT, bool LISTED = false>
+// values, weighted sums (NR weight columns), rechecks of the flagged pairs.
+// Adds the row sums of these columns to racc[r], and to bsk the columns' sum
+// of |w| (over the weight columns) where every value of the 32 columns lies
+// below 2^-96.  The 32 columns are summed in FP32 (four interleaved partial
+// sums) and enter the FP64 row sum with one conversion and one add: FP64
+// instructions issue at a small fraction of the FP32 rate here.
+template <int KT, bool LISTED, int NR>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
                                               const SrcMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
-                                              bool gfast, const LTab &ltab, double &racc,
+                                              bool gfast, const LTab &ltab, double (&racc)[NR],
                                               float &bsk, float *wq)
 {
   // Gaussian kinds with the pools' float-pair copies: flagged pairs are
   // collected over the 32 columns (fl32) and rechecked by the whole warp
   constexpr bool GK = KT == KS_GAUSSIAN || KT == KS_GAUSSIAN_VAR_BANDWIDTH;
   uint32_t fl32 = 0;
-  float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  double rchk = 0.0;
+  float acc[NR][4];
+#pragma unroll
+  for (int r = 0; r < NR; r++) acc[r][0] = acc[r][1] = acc[r][2] = acc[r][3] = 0.f;
+  double rchk[NR];
+#pragma unroll
+  for (int r = 0; r < NR; r++) rchk[r] = 0.0;
   float fchk = 0.f;                 // |rechecked values|, for the underflow test
   bool nchk = false;
   float amin = gfast ? 0.f : 3.0e38f;   // see epi_chunk (not tracked by the Gaussian fast path)
@@ -1587,8 +1678,8 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   // it may flag pairs)
   const bool ffp = a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag);
   // columns per TMEM load: 8 for the kernels with the most live state per column (the list
-  // form's Laplace too: its kernel holds every epilogue variant)
-  constexpr int NCH = (KT == KS_GAUSSIAN_VAR_BANDWIDTH || (KT == KS_LAPLACE && LISTED)) ? 8 : 16;
+  // form's Laplace too: its kernel holds every epilogue variant; and several weight columns)
+  constexpr int NCH = (KT == KS_GAUSSIAN_VAR_BANDWIDTH || (KT == KS_LAPLACE && LISTED) || NR > 1) ? 8 : 16;
 #pragma unroll 1
   for (int part = 0; part < 32 / NCH; part++) {
     const int c0 = grp * 32 + part * NCH;
@@ -1597,17 +1688,17 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     tmem_ld<NCH>(tH + 128 + c0, l);
     tmem_ld_wait();
     if constexpr (KT == KS_GAUSSIAN) {
-      if (gfast) { epi_chunk_gfast<NCH>(h, l, bm, c0, am.n_hi, rc, acc); continue; }
+      if (gfast) { epi_chunk_gfast<NCH, NR>(h, l, bm, c0, am.n_hi, rc, acc); continue; }
     }
     if constexpr (kt_uses_norms(KT)) {
       uint32_t flags = 0;
       const bool fl = T.any_flag != 0;
       if (exact) {
-        if (fl) flags = epi_chunk<KT, true, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
-        else epi_chunk<KT, true, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        if (fl) flags = epi_chunk<KT, true, true, NCH, NR>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        else epi_chunk<KT, true, false, NCH, NR>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
       } else {
-        if (fl) flags = epi_chunk<KT, false, true, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
-        else epi_chunk<KT, false, false, NCH>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        if (fl) flags = epi_chunk<KT, false, true, NCH, NR>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        else epi_chunk<KT, false, false, NCH, NR>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
       }
       if constexpr (GK) {
         if (ffp) {
@@ -1621,28 +1712,33 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
         flags &= flags - 1;
         const int c = c0 + j;
         if (c < ncols && am.pos >= 0) {
-          const double v = recheck<KT>(a, T, ltab, am.pos, bm->pos[c]);
+          const int jpos = bm->pos[c];
+          const double kv = recheck<KT>(a, T, ltab, am.pos, jpos);
           if (a.nrecheck) atomicAdd(a.nrecheck, 1ull);
-          rchk += v;
-          fchk += fabsf((float)v);
+#pragma unroll
+          for (int r = 0; r < NR; r++) {
+            const double v = kv * wcol64(a, jpos, r);
+            rchk[r] += v;
+            fchk += fabsf((float)v);
+          }
           nchk = true;
         }
       }
     } else if constexpr (KT == KS_POLYNOMIAL) {
       const int pw = T.kp.pmode == POW_INT ? T.kp.pint : 0;
       if (T.anch) {
-        if (pw == 3) epi_chunk_anchor<NCH, 3>(h, l, bm, c0, am, T.sg, acc);
-        else if (pw == 2) epi_chunk_anchor<NCH, 2>(h, l, bm, c0, am, T.sg, acc);
-        else if (pw == 4) epi_chunk_anchor<NCH, 4>(h, l, bm, c0, am, T.sg, acc);
-        else epi_chunk_anchor<NCH, 1>(h, l, bm, c0, am, T.sg, acc);
+        if (pw == 3) epi_chunk_anchor<NCH, 3, NR>(h, l, bm, c0, am, T.sg, acc);
+        else if (pw == 2) epi_chunk_anchor<NCH, 2, NR>(h, l, bm, c0, am, T.sg, acc);
+        else if (pw == 4) epi_chunk_anchor<NCH, 4, NR>(h, l, bm, c0, am, T.sg, acc);
+        else epi_chunk_anchor<NCH, 1, NR>(h, l, bm, c0, am, T.sg, acc);
       }
-      else if (pw == 2) epi_chunk_ip<KT, NCH, 2>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
-      else if (pw == 3) epi_chunk_ip<KT, NCH, 3>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
-      else if (pw == 4) epi_chunk_ip<KT, NCH, 4>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
-      else if (pw == 1) epi_chunk_ip<KT, NCH, 1>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
-      else epi_chunk_ip<KT, NCH>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else if (pw == 2) epi_chunk_ip<KT, NCH, NR, 2>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else if (pw == 3) epi_chunk_ip<KT, NCH, NR, 3>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else if (pw == 4) epi_chunk_ip<KT, NCH, NR, 4>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else if (pw == 1) epi_chunk_ip<KT, NCH, NR, 1>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else epi_chunk_ip<KT, NCH, NR>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
     } else {
-      epi_chunk_ip<KT, NCH>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      epi_chunk_ip<KT, NCH, NR>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
     }
   }
   if constexpr (GK) {
@@ -1651,13 +1747,21 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
       if (am.pos < 0 || nv <= 0) fl32 = 0;
       else if (nv < 32) fl32 &= (1u << nv) - 1u;
       if (__any_sync(0xffffffffu, fl32 != 0)) {
-        float add = 0.f;
-        recheck_warp<KT>(a, T, am, bm, grp, fl32, wq, add, fchk);
-        acc[0] += add;
+        float add[NR];
+#pragma unroll
+        for (int r = 0; r < NR; r++) add[r] = 0.f;
+        recheck_warp<KT, NR>(a, T, am, bm, grp, fl32, wq, add, fchk);
+#pragma unroll
+        for (int r = 0; r < NR; r++) acc[r][0] += add[r];
       }
     }
   }
-  const float fs = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  float fs[NR], fsa = 0.f;
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    fs[r] = (acc[r][0] + acc[r][1]) + (acc[r][2] + acc[r][3]);
+    fsa += fabsf(fs[r]);
+  }
   if constexpr (kt_rescue(KT)) {
     // Kernel values over these 32 columns all below 2^-96 (FP32 flushes values
     // below 2^-126 to zero, FP64 keeps them down to 2^-1074): the columns add
@@ -1666,28 +1770,33 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
     // the reduction redoes the rows where it may matter (split_rescue,
     // list_rescue).
     const float W = bm->wsum[grp * 32];
-    if (am.pos >= 0 && fabsf(fs) + fchk < 0x1p-96f * W && (KT == KS_LAPLACE || amin < 1111.0f)) bsk += W;
+    if (am.pos >= 0 && fsa + fchk < 0x1p-96f * W && (KT == KS_LAPLACE || amin < 1111.0f)) bsk += W;
   }
-  racc += (double)fs;
-  if (nchk) racc += rchk;
+#pragma unroll
+  for (int r = 0; r < NR; r++) {
+    racc[r] += (double)fs[r];
+    if (nchk) racc[r] += rchk[r];
+  }
 }
 
-template <int KT>
+// NR: weight columns of one sweep (1, or RMAX for several right-hand sides;
+// the list form takes 1).
+template <int KT, int NR>
 __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
 {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *sm = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int kpad = a.kpad;
-  const SmemLayout L = smem_layout(kpad, KT);
+  const SmemLayout L = smem_layout(kpad, KT, NR);
   const bool resident = L.resident;
-  const size_t a_bytes = tile_bytes(BM, kpad), b_bytes = tile_bytes(BN, kpad);
+  const size_t a_bytes = tile_bytes(BM, kpad), b_bytes = tile_bytes(BN, kpad, smeta_pt(NR));
   const size_t a_op = NBLK * blk_bytes(BM, kpad);     // operand part of a tile image
   const size_t meta_bytes = (size_t)BM * sizeof(PtMeta);
   uint8_t *sA = sm;                                   // target image (resident) or target meta
   uint8_t *sAmeta = resident ? sA + a_op : sA;
   uint8_t *sStage = sm + L.a_region;
   uint8_t *sBm = sStage + L.nstage * L.stage_bytes;   // NMETA source metadata slots
-  SplitSmem *S = (SplitSmem *)(sBm + NMETA * meta_bytes);
+  SplitSmem *S = (SplitSmem *)(sBm + NMETA * L.smeta);
   volatile int *abort = &S->abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1775,8 +1884,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           if (stop) break;
           const int ms = tt % NMETA, mu = tt / NMETA;
           if (mu > 0 && !mbar_wait(&S->m_empty[ms], (mu - 1) & 1, abort, a.wait_limit)) break;
-          mbar_arrive_expect_tx(&S->m_full[ms], (uint32_t)meta_bytes);
-          bulk_g2s(sBm + ms * meta_bytes, imgB + a_op, (uint32_t)meta_bytes, &S->m_full[ms]);
+          mbar_arrive_expect_tx(&S->m_full[ms], (uint32_t)L.smeta);
+          bulk_g2s(sBm + ms * L.smeta, imgB + a_op, (uint32_t)L.smeta, &S->m_full[ms]);
           m_last[ms] = mu;
         }
         item = next;
@@ -1869,7 +1978,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       const PtMeta am = ((const PtMeta *)sAmeta)[row];
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->a_empty);
-      double racc = 0.0;
+      double racc[NR];
+#pragma unroll
+      for (int r = 0; r < NR; r++) racc[r] = 0.0;
       float bsk = 0.0f;
       bool ok = true;
       for (int tj = G.t0; tj < G.t1; tj++, g++, tc++) {
@@ -1877,7 +1988,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
         if (!mbar_wait(&S->t_full[buf], (tc >> 1) & 1, abort, a.wait_limit)) { ok = false; break; }
         if (!mbar_wait(&S->m_full[ms], (g / NMETA) & 1, abort, a.wait_limit)) { ok = false; break; }
         tc_fence_after();
-        const SrcMeta *bm = (const SrcMeta *)(sBm + ms * meta_bytes);
+        const SrcMeta *bm = (const SrcMeta *)(sBm + ms * L.smeta);
         const int ncols = a.tab ? a.btile_cols[tj] : min(BN, a.n - tj * BN);
         const uint32_t tH = tmem + ((uint32_t)(qd * 32) << 16) + buf * 256;
         if constexpr (KT == KS_LIST) {
@@ -1885,30 +1996,44 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           const bool lexact = T.exact != 0;
           switch (T.kp.type) {
             case KS_GAUSSIAN:   // scaled units, as a single call
-              tile_epilogue<KS_GAUSSIAN>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_GAUSSIAN, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, ltab, racc, bsk, wq); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_POLYNOMIAL:
-              tile_epilogue<KS_POLYNOMIAL>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_POLYNOMIAL, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE, true>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_LAPLACE, true, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_TANH:
-              tile_epilogue<KS_TANH>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_TANH, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_QUARTIC:
-              tile_epilogue<KS_QUARTIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_QUARTIC, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             case KS_MULTIQUADRATIC:
-              tile_epilogue<KS_MULTIQUADRATIC>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_MULTIQUADRATIC, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
             default:
-              tile_epilogue<KS_EPANECHNIKOV>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_EPANECHNIKOV, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
           }
         } else {
-          tile_epilogue<KT>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, ltab, racc, bsk, wq);
+          tile_epilogue<KT, false, NR>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, ltab, racc, bsk, wq);
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) { mbar_arrive(&S->t_empty[buf]); mbar_arrive(&S->m_empty[ms]); }
       }
       if (!ok) break;
+      if constexpr (NR > 1) {
+        // several right-hand sides: every group writes its own partials (no
+        // exchange): partial[((r nsc + sc) groups + grp) ldp + i], pskip
+        // [(sc groups + grp) ldp + i]; the reduction adds them in that order
+        const bool rowf = KT == KS_GAUSSIAN && gfast;   // the row's low-norm factor
+        const long long sc = G.t0 / a.chunk_tiles, i = (long long)G.ti * BM + row;
+        if (row < G.rows) {
+#pragma unroll
+          for (int r = 0; r < NR; r++)
+            a.partial[((r * a.nsc + sc) * EPI_GROUPS + grp) * a.ldp + i] = rowf ? racc[r] * (double)am.h : racc[r];
+          if (a.pskip) a.pskip[(sc * EPI_GROUPS + grp) * a.ldp + i] = rowf ? bsk * am.h : bsk;
+        }
+        continue;
+      }
       // Combine the groups' row sums in group order, through a slot per item
       // parity: groups 1.. write theirs and arrive on r_full, group 0 waits,
       // reads and arrives on r_empty.  Every wait is bounded (a block-wide
@@ -1918,20 +2043,20 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       float (*xb)[BM] = S->rskip[rb];
       if (grp > 0) {
         if (ru > 0 && !mbar_wait(&S->r_empty[rb], (ru - 1) & 1, abort, a.wait_limit)) break;
-        xs[grp - 1][row] = racc;
+        xs[grp - 1][row] = racc[0];
         xb[grp - 1][row] = bsk;
         mbar_arrive(&S->r_full[rb]);
       } else {
         if (!mbar_wait(&S->r_full[rb], ru & 1, abort, a.wait_limit)) break;
-        for (int q = 0; q < EPI_GROUPS - 1; q++) { racc += xs[q][row]; bsk += xb[q][row]; }
+        for (int q = 0; q < EPI_GROUPS - 1; q++) { racc[0] += xs[q][row]; bsk += xb[q][row]; }
         mbar_arrive(&S->r_empty[rb]);
         const bool rowf = KT == KS_LIST ? (T.kp.type == KS_GAUSSIAN && T.gfast != 0) : (KT == KS_GAUSSIAN && gfast);
         if (rowf) {                               // the row's low-norm factor
-          racc *= (double)am.h;
+          racc[0] *= (double)am.h;
           bsk *= am.h;
         }
         if (row < G.rows) {
-          a.partial[G.out + row] = racc;
+          a.partial[G.out + row] = racc[0];
           if (a.pskip) a.pskip[G.out + row] = bsk;
         }
       }
@@ -1949,32 +2074,61 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
 // 2^-96 b.  Where that could reach 2^-27 of |s| (in practice: rows whose
 // every value is that small) the row goes to the rescue list instead.
 // Anchored polynomial rows (rowc != nullptr): the row's v0^p times the sum of
-// all weights, *wsum, is added in FP64.
+// all weights, wsum[r], is added in FP64.
+// NR > 1 (several right-hand sides, nrhs <= NR interleaved in u): the
+// partials of every (column r, chunk, epilogue group), in that order; a row is
+// rescued when the skipped groups could matter for any of its columns.
+template <int NR>
 __global__ void split_reduce(int m, int nsc, int ldp, const double *__restrict__ partial,
                              const float *__restrict__ pskip, double *__restrict__ u, const int *__restrict__ umap,
                              int *__restrict__ rlist, int *__restrict__ rcount, const double *__restrict__ rowc,
-                             const double *__restrict__ wsum)
+                             const double *__restrict__ wsum, int nrhs)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
-  double s = 0.0;
-  float b = 0.0f;
-  for (int c = 0; c < nsc; c++) s += partial[(size_t)c * ldp + i];
-  if (rowc) s += rowc[i] * *wsum;
-  if (pskip) {
-    for (int c = 0; c < nsc; c++) b += pskip[(size_t)c * ldp + i];
-    if (b > 0.0f && fabs(s) < 0x1p-69 * (double)b) {
-      rlist[atomicAdd(rcount, 1)] = i;
-      return;
+  if constexpr (NR == 1) {
+    double s = 0.0;
+    float b = 0.0f;
+    for (int c = 0; c < nsc; c++) s += partial[(size_t)c * ldp + i];
+    if (rowc) s += rowc[i] * *wsum;
+    if (pskip) {
+      for (int c = 0; c < nsc; c++) b += pskip[(size_t)c * ldp + i];
+      if (b > 0.0f && fabs(s) < 0x1p-69 * (double)b) {
+        rlist[atomicAdd(rcount, 1)] = i;
+        return;
+      }
     }
+    u[umap ? umap[i] : i] += s;
+  } else {
+    double s[NR];
+    double smin = 1e300;
+#pragma unroll
+    for (int r = 0; r < NR; r++) {
+      s[r] = 0.0;
+      if (r >= nrhs) continue;
+      for (int c = 0; c < nsc * EPI_GROUPS; c++) s[r] += partial[((size_t)r * nsc * EPI_GROUPS + c) * ldp + i];
+      if (rowc) s[r] += rowc[i] * wsum[r];
+      smin = fmin(smin, fabs(s[r]));
+    }
+    if (pskip) {
+      float b = 0.0f;
+      for (int c = 0; c < nsc * EPI_GROUPS; c++) b += pskip[(size_t)c * ldp + i];
+      if (b > 0.0f && smin < 0x1p-69 * (double)b) {
+        rlist[atomicAdd(rcount, 1)] = i;
+        return;
+      }
+    }
+    const size_t ui = (size_t)(umap ? umap[i] : i) * nrhs;
+#pragma unroll
+    for (int r = 0; r < NR; r++)
+      if (r < nrhs) u[ui + r] += s[r];
   }
-  u[umap ? umap[i] : i] += s;
 }
 
 // The rows of the rescue list, one warp per row: every pair of the row from
 // the pool coordinates (recheck: float-pair distances, values in the FP64
 // range), summed in FP64 in a fixed order.
-template <int KT>
+template <int KT, int NR>
 __global__ void __launch_bounds__(256) split_rescue(TileArgs a, const int *__restrict__ rlist,
                                                     const int *__restrict__ rcount, double *__restrict__ u,
                                                     const int *__restrict__ umap)
@@ -1995,28 +2149,46 @@ __global__ void __launch_bounds__(256) split_rescue(TileArgs a, const int *__res
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < nr; e += nw) {
     const int i = rlist[e];
-    double r = 0.0;
-    for (int j = lane; j < a.n; j += 32) r += recheck<KT, true>(a, T, ltab, i, j);
+    const int nr = a.nrhs > 1 ? a.nrhs : 1;
+    double r[NR];
 #pragma unroll
-    for (int o = 16; o; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-    if (lane == 0) u[umap ? umap[i] : i] += r;
+    for (int q = 0; q < NR; q++) r[q] = 0.0;
+    for (int j = lane; j < a.n; j += 32) {
+      const double kv = recheck<KT, true>(a, T, ltab, i, j);
+#pragma unroll
+      for (int q = 0; q < NR; q++)
+        if (q < nr) r[q] += kv * wcol64(a, j, q);
+    }
+#pragma unroll
+    for (int q = 0; q < NR; q++) {
+#pragma unroll
+      for (int o = 16; o; o >>= 1) r[q] += __shfl_xor_sync(0xffffffffu, r[q], o);
+      if (lane == 0 && q < nr) u[(size_t)(umap ? umap[i] : i) * nr + q] += r[q];
+    }
   }
 }
 
-cudaError_t launch_rescue(const TileArgs &a, int grid, const int *rlist, const int *rcount, double *u,
-                          const int *umap, cudaStream_t s)
+template <int NR>
+cudaError_t launch_rescue_t(const TileArgs &a, int grid, const int *rlist, const int *rcount, double *u,
+                            const int *umap, cudaStream_t s)
 {
   switch (a.kt) {
-    case KS_GAUSSIAN: split_rescue<KS_GAUSSIAN><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
+    case KS_GAUSSIAN: split_rescue<KS_GAUSSIAN, NR><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
     case KS_GAUSSIAN_VAR_BANDWIDTH:
-      split_rescue<KS_GAUSSIAN_VAR_BANDWIDTH><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
-    case KS_LAPLACE: split_rescue<KS_LAPLACE><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
+      split_rescue<KS_GAUSSIAN_VAR_BANDWIDTH, NR><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
+    case KS_LAPLACE: split_rescue<KS_LAPLACE, NR><<<grid, 256, 0, s>>>(a, rlist, rcount, u, umap); break;
     default: return cudaSuccess;
   }
   return cudaGetLastError();
 }
+cudaError_t launch_rescue(const TileArgs &a, int grid, const int *rlist, const int *rcount, double *u,
+                          const int *umap, cudaStream_t s, int nr)
+{
+  return nr > 1 ? launch_rescue_t<RMAX>(a, grid, rlist, rcount, u, umap, s)
+                : launch_rescue_t<1>(a, grid, rlist, rcount, u, umap, s);
+}
 
-template <int KT>
+template <int KT, int NR>
 cudaError_t launch_tiles_t(const TileArgs &a, int grid, size_t smem, cudaStream_t s)
 {
   // The attribute is per function and device; raise it to what this launch needs.
@@ -2024,32 +2196,39 @@ cudaError_t launch_tiles_t(const TileArgs &a, int grid, size_t smem, cudaStream_
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64 || attr_bytes[dev] < (int)smem) {
-    cudaError_t e = cudaFuncSetAttribute(split_tiles<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(split_tiles<KT, NR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (dev >= 0 && dev < 64) attr_bytes[dev] = (int)smem;
   }
-  split_tiles<KT><<<grid, NTHREADS, smem, s>>>(a);
+  split_tiles<KT, NR><<<grid, NTHREADS, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tiles(const TileArgs &a, int grid, size_t smem, cudaStream_t s)
+template <int NR>
+cudaError_t launch_tiles_nr(const TileArgs &a, int grid, size_t smem, cudaStream_t s)
 {
   switch (a.kt) {
-    case KS_GAUSSIAN: return launch_tiles_t<KS_GAUSSIAN>(a, grid, smem, s);
-    case KS_GAUSSIAN_VAR_BANDWIDTH: return launch_tiles_t<KS_GAUSSIAN_VAR_BANDWIDTH>(a, grid, smem, s);
-    case KS_POLYNOMIAL: return launch_tiles_t<KS_POLYNOMIAL>(a, grid, smem, s);
-    case KS_LAPLACE: return launch_tiles_t<KS_LAPLACE>(a, grid, smem, s);
-    case KS_TANH: return launch_tiles_t<KS_TANH>(a, grid, smem, s);
-    case KS_QUARTIC: return launch_tiles_t<KS_QUARTIC>(a, grid, smem, s);
-    case KS_MULTIQUADRATIC: return launch_tiles_t<KS_MULTIQUADRATIC>(a, grid, smem, s);
-    case KS_LIST: return launch_tiles_t<KS_LIST>(a, grid, smem, s);
-    default: return launch_tiles_t<KS_EPANECHNIKOV>(a, grid, smem, s);
+    case KS_GAUSSIAN: return launch_tiles_t<KS_GAUSSIAN, NR>(a, grid, smem, s);
+    case KS_GAUSSIAN_VAR_BANDWIDTH: return launch_tiles_t<KS_GAUSSIAN_VAR_BANDWIDTH, NR>(a, grid, smem, s);
+    case KS_POLYNOMIAL: return launch_tiles_t<KS_POLYNOMIAL, NR>(a, grid, smem, s);
+    case KS_LAPLACE: return launch_tiles_t<KS_LAPLACE, NR>(a, grid, smem, s);
+    case KS_TANH: return launch_tiles_t<KS_TANH, NR>(a, grid, smem, s);
+    case KS_QUARTIC: return launch_tiles_t<KS_QUARTIC, NR>(a, grid, smem, s);
+    case KS_MULTIQUADRATIC: return launch_tiles_t<KS_MULTIQUADRATIC, NR>(a, grid, smem, s);
+    default: return launch_tiles_t<KS_EPANECHNIKOV, NR>(a, grid, smem, s);
   }
 }
 
-size_t smem_bytes(int kpad, int kt)
+// nr: weight columns of the sweep (1, or RMAX); the list form takes one.
+cudaError_t launch_tiles(const TileArgs &a, int grid, size_t smem, cudaStream_t s, int nr = 1)
 {
-  const SmemLayout L = smem_layout(kpad, kt);
+  if (a.kt == KS_LIST) return launch_tiles_t<KS_LIST, 1>(a, grid, smem, s);
+  return nr > 1 ? launch_tiles_nr<RMAX>(a, grid, smem, s) : launch_tiles_nr<1>(a, grid, smem, s);
+}
+
+size_t smem_bytes(int kpad, int kt, int nr = 1)
+{
+  const SmemLayout L = smem_layout(kpad, kt, nr);
   return smem_fixed(L) + (L.tab_sh >= 0 ? ((size_t)LTAB << L.tab_sh) * 16 : 0);
 }
 
@@ -2064,13 +2243,18 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
                   const double *XA, const double *XA2, const int *amap, int nxa,
                   const double *XB, const double *XB2, const int *bmap, int nxb,
                   const double *w, const int *wmap, const double *hi, const double *hj,
-                  cudaStream_t s, bool stream_ordered_alloc)
+                  cudaStream_t s, bool stream_ordered_alloc, int nrhs)
 {
   using namespace split;
   (void)XA2; (void)XB2;
+  // several right-hand sides (u, w with nrhs interleaved columns, nrhs <= RMAX)
+  // in one sweep: every kernel value times each weight column
+  if (nrhs < 1 || nrhs > RMAX) return GSKS_ERR_ARG;
+  const int NRK = nrhs > 1 ? RMAX : 1;   // weight columns of the kernel
   // padded k: a multiple of the MMA k-step (16) up to one chunk, of the chunk beyond
   const int kpad = k <= KCH ? (k + 15) / 16 * 16 : (k + KCH - 1) / KCH * KCH;
   if (kpad > 1024) return GSKS_ERR_TOO_LARGE;   // the exact head accumulation needs k <= 1024
+  if (smem_bytes(kpad, ker->type, NRK) > SMEM_MAX) return GSKS_ERR_TOO_LARGE;
   const int ntm = (m + BM - 1) / BM, ntn = (n + BN - 1) / BN;
   const int sms = std::max(1, c->num_sms);
   // decomposition: the source tiles of a target tile split into nsc chunks of
@@ -2100,7 +2284,10 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const size_t o_bbox = o_centre + al((size_t)k * 8);
   const size_t o_a = o_bbox + al((size_t)2 * k * 8);
   const size_t o_b = o_a + al((size_t)ntm * tile_bytes(BM, kpad));
-  const size_t o_p = o_b + al((size_t)ntn * tile_bytes(BN, kpad));
+  const size_t o_p = o_b + al((size_t)ntn * tile_bytes(BN, kpad, smeta_pt(NRK)));
+  // partial sums: [nsc][ldp], or with several columns [RMAX][nsc][groups][ldp]
+  const size_t nparts = NRK > 1 ? (size_t)RMAX * nsc * EPI_GROUPS * ldp : (size_t)nsc * ldp;
+  const size_t nskips = NRK > 1 ? (size_t)nsc * EPI_GROUPS * ldp : (size_t)nsc * ldp;
   // float-pair copies for cheap rechecks (kernels with rechecks; written only
   // when the call may flag pairs): of the pool when the targets and sources
   // share one whose points are no more than the gathered ones (indexed by
@@ -2111,8 +2298,8 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const long long ffa = ffpos ? m : nxa, ffb = ffpos ? n : (same_pool ? 0 : nxb);   // points per copy
   // row rescue (exponential kernels): skipped-group weights, row list, count
   const bool defer = kt_rescue(ker->type);
-  const size_t o_ps = o_p + al((size_t)nsc * ldp * 8);
-  const size_t o_rl = o_ps + (defer ? al((size_t)nsc * ldp * 4) : 0);
+  const size_t o_ps = o_p + al(nparts * 8);
+  const size_t o_rl = o_ps + (defer ? al(nskips * 4) : 0);
   const size_t o_rc = o_rl + (defer ? al((size_t)m * 4) : 0);
   const size_t o_ni = o_rc + (defer ? al(4) : 0);   // work counter
   const size_t o_xaf = o_ni + al(4);
@@ -2123,7 +2310,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
                     ker->powe <= 4.0;
   const int nwb = (n + ANCHOR_WPER - 1) / ANCHOR_WPER;   // blocks of the weight sum
   const size_t o_anc = o_xbf + (ff ? al((size_t)ffb * k * sizeof(float2)) : 0);
-  const size_t o_rowc = o_anc + (anch ? al(((size_t)k + 1 + (size_t)nwb) * 8) : 0);
+  const size_t o_rowc = o_anc + (anch ? al(((size_t)k + RMAX + (size_t)nwb * nrhs) * 8) : 0);
   const size_t total = o_rowc + (anch ? al((size_t)m * 8) : 0);
   uint8_t *ws = nullptr;
   if (stream_ordered_alloc) {
@@ -2152,15 +2339,15 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   params_kernel<<<1, 1024, 0, s>>>(k, ker->type, ker->scal, ker->cons, ker->powe, tau, bbox, centre, P);
   double *ybar = anch ? (double *)(ws + o_anc) : nullptr;
   double *rowc = anch ? (double *)(ws + o_rowc) : nullptr;
-  if (anch) {   // ybar[k] | wsum | the weight-sum blocks' partials
-    anchor_partial<<<(k + 31) / 32 + nwb, 256, 0, s>>>(n, k, XB, bmap, nxb, w, wmap, err_word(c), ybar,
-                                                      ybar + k + 1);
-    anchor_final<<<1, 32, 0, s>>>(nwb, ybar + k + 1, ybar + k);
+  if (anch) {   // ybar[k] | wsum[RMAX] | the weight-sum blocks' partials
+    anchor_partial<<<(k + 31) / 32 + nwb, 256, 0, s>>>(n, k, XB, bmap, nxb, w, wmap, nrhs, err_word(c), ybar,
+                                                      ybar + k + RMAX);
+    anchor_final<<<1, 32, 0, s>>>(nwb, nrhs, ybar + k + RMAX, ybar + k);
   }
   pack_kernel<<<ntm, BM, 0, s>>>(0, m, k, kpad, XA, amap, nxa, err_word(c), nullptr, nullptr, hi, ker->type,
                                  centre, P, ws + o_a, nullptr, nullptr, nullptr, ybar, rowc);
   pack_kernel<<<ntn, BN, 0, s>>>(1, n, k, kpad, XB, bmap, nxb, err_word(c), w, wmap, hj, ker->type, centre,
-                                 P, ws + o_b, nullptr, nullptr, nullptr, nullptr, nullptr);
+                                 P, ws + o_b, nullptr, nullptr, nullptr, nullptr, nullptr, nrhs);
 
   TileArgs a{};
   a.m = m; a.n = n; a.k = k; a.kpad = kpad; a.kt = ker->type;
@@ -2191,6 +2378,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   a.err = err_word(c);
   a.wait_limit = tl_split_wait > 0 ? tl_split_wait : WAIT_LIMIT;
   a.stall = tl_split_stall;
+  a.nrhs = nrhs;
   const int grid = std::min(ntm * nsc, sms);
   int *rlist = defer ? (int *)(ws + o_rl) : nullptr, *rcount = defer ? (int *)(ws + o_rc) : nullptr;
   // diagnostics of this call (gsks_split_stats): rechecked pairs, rescued rows
@@ -2202,15 +2390,20 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   cudaError_t e = cudaMemsetAsync(c->stats.p, 0, 16, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(a.next_item, 0, sizeof(int), s);
   if (e == cudaSuccess && defer) e = cudaMemsetAsync(rcount, 0, sizeof(int), s);
-  if (e == cudaSuccess) e = launch_tiles(a, grid, smem_bytes(kpad, a.kt), s);
+  if (e == cudaSuccess) e = launch_tiles(a, grid, smem_bytes(kpad, a.kt, NRK), s, NRK);
   if (e == cudaSuccess) {
-    split_reduce<<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, a.pskip, u, umap, rlist, rcount, rowc,
-                                                 anch ? ybar + k : nullptr);
+    if (NRK > 1)
+      split_reduce<RMAX><<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, a.pskip, u, umap, rlist, rcount,
+                                                         rowc, anch ? ybar + k : nullptr, nrhs);
+    else
+      split_reduce<1><<<(m + 255) / 256, 256, 0, s>>>(m, nsc, ldp, a.partial, a.pskip, u, umap, rlist, rcount, rowc,
+                                                      anch ? ybar + k : nullptr, 1);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && defer)
     e = cudaMemcpyAsync((uint8_t *)c->stats.p + 8, rcount, sizeof(int), cudaMemcpyDeviceToDevice, s);
-  if (e == cudaSuccess && defer) e = launch_rescue(a, std::max(1, std::min(2 * sms, (m + 7) / 8)), rlist, rcount, u, umap, s);
+  if (e == cudaSuccess && defer)
+    e = launch_rescue(a, std::max(1, std::min(2 * sms, (m + 7) / 8)), rlist, rcount, u, umap, s, NRK);
   if (stream_ordered_alloc) cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_status(e, "split launch");
   note_launches((defer ? 8 : 7) + ff_launches + (anch ? 2 : 0));
@@ -2282,11 +2475,13 @@ __global__ void __launch_bounds__(256) list_rescue(TileArgs a, int ntask, const 
     const TaskParam &T = a.tp[t];
     double r = 0.0;
     for (int j = G.b0 + lane; j < G.b0 + G.n; j += 32) {
+      double kv;
       switch (T.kp.type) {
-        case KS_GAUSSIAN: r += recheck<KS_GAUSSIAN, true>(a, T, ltab, pos, j); break;
-        case KS_GAUSSIAN_VAR_BANDWIDTH: r += recheck<KS_GAUSSIAN_VAR_BANDWIDTH, true>(a, T, ltab, pos, j); break;
-        default: r += recheck<KS_LAPLACE, true>(a, T, ltab, pos, j); break;
+        case KS_GAUSSIAN: kv = recheck<KS_GAUSSIAN, true>(a, T, ltab, pos, j); break;
+        case KS_GAUSSIAN_VAR_BANDWIDTH: kv = recheck<KS_GAUSSIAN_VAR_BANDWIDTH, true>(a, T, ltab, pos, j); break;
+        default: kv = recheck<KS_LAPLACE, true>(a, T, ltab, pos, j); break;
       }
+      r += kv * wcol64(a, j, 0);
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
@@ -2506,6 +2701,7 @@ int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int 
   a.pskip = (float *)(ws + Pl.o_pskip);
   a.next_item = (int *)(ws + Pl.o_ni);
   a.err = err;
+  a.nrhs = 1;
   a.wait_limit = tl_split_wait > 0 ? tl_split_wait : WAIT_LIMIT;
   a.stall = tl_split_stall;
   a.tab = (const SplitItem *)(ws + Pl.o_items);
