@@ -432,7 +432,8 @@ __global__ void params_kernel(int k, int kt, double scal, double cons, double po
     P->exact_t1 = (q <= 2.0 * sigma * sigma * 0x1p-14) ? 1 : 0;
     P->gfast = (kt == KS_GAUSSIAN && P->exact_t1 && !P->any_flag) ? 1 : 0;
     P->ff_ok = (s_mx[0] <= 0x1p50) ? 1 : 0;
-    P->anch = (kt == KS_POLYNOMIAL && powe == rint(powe) && powe >= 1.0 && powe <= 4.0) ? 1 : 0;
+    P->anch = ((kt == KS_POLYNOMIAL && powe == rint(powe) && powe >= 1.0 && powe <= 4.0) || kt == KS_TANH ||
+               kt == KS_QUARTIC || kt == KS_MULTIQUADRATIC || kt == KS_EPANECHNIKOV) ? 1 : 0;
     P->sg = (float)(scal * 0.5 * P->g);
     P->pw = (int)powe;
     P->pscal = scal;
@@ -475,7 +476,8 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   T.rc = (float)(-g);
   T.exact = (q <= g) ? 1 : 0;
   T.gfast = 0;
-  T.anch = (kp.type == KS_POLYNOMIAL && kp.pmode == POW_INT && kp.pint >= 1 && kp.pint <= 4) ? 1 : 0;
+  T.anch = ((kp.type == KS_POLYNOMIAL && kp.pmode == POW_INT && kp.pint >= 1 && kp.pint <= 4) ||
+            kp.type == KS_TANH) ? 1 : 0;
   T.sg = (float)(kp.scal * 0.5 * g);
   T.pad = 0;
   if (kp.type == KS_GAUSSIAN) {
@@ -554,8 +556,9 @@ __device__ void block_source_sums(int j0, int j1, int k, const double *__restric
   }
 }
 
-// Anchor point of a single call's polynomial kernel and the sum of all
-// weights.  Any point inside the sources' hull keeps each row's anchor value
+// Anchor point of a single call's polynomial, tanh and compact / multiquadratic
+// kernels (the sources' mean and mean squares per coordinate) and the sum of
+// all weights.  Any point inside the sources' hull keeps each row's anchor value
 // within the range of that row's values, so the mean of a strided sample of
 // at most ANCHOR_SAMPLE sources serves (blocks 0 .. ceil(k/32)-1: 32
 // coordinates each, 8 warps over the sample, combined in warp order).  The
@@ -569,7 +572,7 @@ __global__ void __launch_bounds__(256) anchor_partial(int n, int k, const double
                                                       const int *__restrict__ bmap, int nxb,
                                                       const double *__restrict__ w, const int *__restrict__ wmap,
                                                       int nrhs, int *err, double *__restrict__ ybar,
-                                                      double *__restrict__ wpart)
+                                                      double *__restrict__ wpart, double *__restrict__ ybsq)
 {
   // nrhs interleaved weight columns: one sum per column (wpart[b nrhs + r])
   __shared__ double sh[256];
@@ -577,10 +580,14 @@ __global__ void __launch_bounds__(256) anchor_partial(int n, int k, const double
   if ((int)blockIdx.x < ncb) {
     const int S = min(n, ANCHOR_SAMPLE), stride = n / S;
     const int p = blockIdx.x * 32 + lane;
-    double s = 0.0;
+    double s = 0.0, s2 = 0.0;
     if (p < k) {
 #pragma unroll 4
-      for (int q = wp; q < S; q += 8) s += XB[(size_t)pool_index(bmap, q * stride, nxb, err) * k + p];
+      for (int q = wp; q < S; q += 8) {
+        const double y = XB[(size_t)pool_index(bmap, q * stride, nxb, err) * k + p];
+        s += y;
+        s2 = fma(y, y, s2);
+      }
     }
     sh[t] = s;
     __syncthreads();
@@ -588,6 +595,14 @@ __global__ void __launch_bounds__(256) anchor_partial(int n, int k, const double
       double r = 0.0;
       for (int q = 0; q < 8; q++) r += sh[q * 32 + lane];
       ybar[p] = r / (double)S;
+    }
+    __syncthreads();
+    sh[t] = s2;
+    __syncthreads();
+    if (wp == 0 && p < k) {   // the sample's mean square of coordinate p (distance kernels' anchors)
+      double r = 0.0;
+      for (int q = 0; q < 8; q++) r += sh[q * 32 + lane];
+      ybsq[p] = r / (double)S;
     }
     return;
   }
@@ -643,7 +658,8 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
                             const double *__restrict__ centre, const Params *__restrict__ P,
                             uint8_t *__restrict__ img, const int2 *__restrict__ tiles,
                             const int *__restrict__ tile_task, const TaskParam *__restrict__ tp,
-                            const double *__restrict__ ybar, double *__restrict__ rowc, int nrhs = 1)
+                            const double *__restrict__ ybar, double *__restrict__ rowc, int nrhs = 1,
+                            const double *__restrict__ ybsq = nullptr)
 {
   // nrhs > 1 (sources of several right-hand sides): w holds nrhs interleaved
   // columns and the tiles carry RMAX weights per point (SrcMetaX)
@@ -741,11 +757,36 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   }
   const bool anch = side == 0 && (TT ? TT->anch != 0 : P->anch != 0);
   if (anch) {
-    // Polynomial rows summed around an anchor: H0 = x.ybar in accumulator
-    // units (x.y = (g/2)(H + L)), rounded to an integer so that H - H0 is
-    // exact, and v0 = cons + scal (g/2) H0; the row keeps H0 (n_hi) and the
-    // binomial coefficients c_i = C(p, i) v0^(p-i), i = 1..p-1 (n_lo, w, h);
-    // rowc gets v0^p in FP64.  Padding rows: all zero.
+    // Polynomial and tanh rows summed around an anchor: H0 = x.ybar in
+    // accumulator units (x.y = (g/2)(H + L)), rounded to an integer so that
+    // H - H0 is exact, and v0 = cons + scal (g/2) H0; the row keeps H0 (n_hi)
+    // and, for the polynomial, the binomial coefficients c_i = C(p, i)
+    // v0^(p-i), i = 1..p-1 (n_lo, w, h), rowc v0^p in FP64; for tanh, t0 =
+    // tanh(v0) and 1 - t0^2 (n_lo, w), rowc t0 in FP64.  Padding rows: zero.
+    if (kt_uses_norms(kt)) {
+      // Compact and multiquadratic kernels (functions of d2): the anchor is
+      // d0^2 = |x - ybar|^2 + mean |y - ybar|^2, the rows' mean squared
+      // distance to the sources; the row keeps d0^2 (w), K(d0^2) in FP32 (h)
+      // and 1 - d0^2 (pad[0]); rowc gets K(d0^2) in FP64.  The norms stay.
+      mt.w = mt.h = 0.0f;
+      mt.pad[0] = 0;
+      if (valid) {
+        double d0 = 0.0;
+        for (int p = 0; p < k; p++) {
+          const double dx = x[p] - ybar[p];
+          d0 = fma(dx, dx, d0) + (ybsq[p] - ybar[p] * ybar[p]);
+        }
+        const double c = 1.0 - d0;
+        double K0;
+        if (kt == KS_QUARTIC) K0 = d0 < 1.0 ? (15.0 / 16.0) * c * c : 0.0;
+        else if (kt == KS_EPANECHNIKOV) K0 = d0 < 1.0 ? 0.75 * c : 0.0;
+        else K0 = d0 + (TT ? TT->kp.cons : P->pcons);
+        mt.w = (float)d0;
+        mt.h = (float)K0;
+        mt.pad[0] = __float_as_int((float)c);
+        rowc[pt] = K0;
+      }
+    } else {
     mt.n_hi = mt.n_lo = mt.w = mt.h = 0.0f;
     if (valid) {
       const double *yb = ybar + (TT ? (size_t)tile_task[tile] * k : 0);
@@ -758,7 +799,8 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
       const double v0 = fma(scal * G, H0, cons);
       const double v2 = v0 * v0;
       double c1 = 1.0, c2 = 0.0, c3 = 0.0, vp = v0;
-      if (pw == 2) { c1 = 2.0 * v0; vp = v2; }
+      if (kt == KS_TANH) { vp = tanh(v0); c1 = vp; c2 = 1.0 - vp * vp; c3 = v0; }
+      else if (pw == 2) { c1 = 2.0 * v0; vp = v2; }
       else if (pw == 3) { c1 = 3.0 * v2; c2 = 3.0 * v0; vp = v2 * v0; }
       else if (pw == 4) { c1 = 4.0 * v2 * v0; c2 = 6.0 * v2; c3 = 4.0 * v0; vp = v2 * v2; }
       mt.n_hi = (float)H0;
@@ -766,6 +808,7 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
       mt.w = (float)c2;
       mt.h = (float)c3;
       rowc[pt] = vp;
+    }
     }
   }
   if (side == 0) {
@@ -1504,6 +1547,20 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
       float kv;
       if constexpr (KT == KS_LAPLACE || KT == KS_GAUSSIAN_VAR_BANDWIDTH)
         kv = (q & 1) ? hi2(KV2[q >> 1]) : lo2(KV2[q >> 1]);
+      else if constexpr (KT == KS_QUARTIC || KT == KS_EPANECHNIKOV || KT == KS_MULTIQUADRATIC) {
+        if (T.anch) {
+          // K - K(d0^2) from e = d2 - d0^2 (t - d0^2 is exact near the anchor)
+          const float e = (t - am.w) + lo;
+          const float d = t + lo, c = __int_as_float(am.pad[0]);
+          if constexpr (KT == KS_MULTIQUADRATIC) kv = e;
+          else if (d >= 1.0f) kv = -am.h;                                       // K = 0
+          else if (c <= 0.0f) kv = kval32<KT>(t, lo, 0.f, 0.f, 0.f, kp);        // K(d0^2) = 0
+          else if constexpr (KT == KS_EPANECHNIKOV) kv = -0.75f * e;
+          else kv = 0.9375f * e * (e - 2.0f * c);
+        } else {
+          kv = kval32<KT>(t, lo, 0.f, am.h, 0.f, kp);
+        }
+      }
       else kv = kval32<KT>(t, lo, 0.f, am.h, 0.f, kp);
       // smallest exponent (log2 units) of the exponential kernels' values: the
       // row rescue is needed only if some value is not 0 in FP64 either
@@ -1641,6 +1698,52 @@ __device__ __forceinline__ void epi_chunk_anchor(const uint32_t (&h)[NC], const 
   }
 }
 
+// tanh in FP32: its series for |v| < 1/8, else from 2^(2 log2(e) |v|).
+__device__ __forceinline__ float tanh32(float v)
+{
+  const float av = fabsf(v);
+  if (av < 0.125f) {
+    const float v2 = v * v;   // v - v^3/3 + 2v^5/15 - 17v^7/315
+    return v * fmaf(v2, fmaf(v2, fmaf(v2, -17.0f / 315.0f, 2.0f / 15.0f), -1.0f / 3.0f), 1.0f);
+  }
+  const float e = ex2_approx(2.0f * 1.44269504f * av);
+  return copysignf(1.0f - 2.0f / (e + 1.0f), v);
+}
+
+// NC columns of one row, tanh summed around the row's anchor v0: with d =
+// v - v0 = sg ((H - H0) + L) and, for |d| < 1/8, tau = tanh(d),
+//   tanh(v) - t0 = tau (1 - t0^2) / (1 + t0 tau),   t0 = tanh(v0)
+// (the addition theorem; the denominator stays above 7/8); farther from the
+// anchor, tanh(v0 + d) - t0 directly.  t0, 1 - t0^2 and v0 come from the
+// row's metadata; the reduction adds t0 times the sum of the weights in FP64.
+template <int NC, int NR>
+__device__ __forceinline__ void epi_chunk_tanh_anchor(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
+                                                      const SrcMeta *__restrict__ bm, int c0, const PtMeta &am,
+                                                      float sg, float (&acc)[NR][4])
+{
+  const float t0 = am.n_lo, s0 = am.w;
+#pragma unroll
+  for (int j4 = 0; j4 < NC; j4 += 4) {
+    float4 ww[NR];
+#pragma unroll
+    for (int r = 0; r < NR; r++) ww[r] = ld4(wrow(bm, r) + c0 + j4);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int j = j4 + q;
+      const float d = ((__uint_as_float(h[j]) - am.n_hi) + __uint_as_float(l[j])) * sg;
+      float kv;
+      if (fabsf(d) < 0.125f) {
+        const float tau = tanh32(d);
+        kv = tau * s0 / fmaf(t0, tau, 1.0f);
+      } else {
+        kv = tanh32(am.h + d) - t0;
+      }
+#pragma unroll
+      for (int r = 0; r < NR; r++) acc[r][q] = fmaf(kv, f4(ww[r], q), acc[r][q]);
+    }
+  }
+}
+
 // Kernels whose FP32 values may fall below the FP32 range while FP64 keeps
 // them (the row rescue of tile_epilogue).
 __host__ __device__ constexpr bool kt_rescue(int kt)
@@ -1736,6 +1839,9 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
       else if (pw == 3) epi_chunk_ip<KT, NCH, NR, 3>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
       else if (pw == 4) epi_chunk_ip<KT, NCH, NR, 4>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
       else if (pw == 1) epi_chunk_ip<KT, NCH, NR, 1>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+      else epi_chunk_ip<KT, NCH, NR>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
+    } else if constexpr (KT == KS_TANH) {
+      if (T.anch) epi_chunk_tanh_anchor<NCH, NR>(h, l, bm, c0, am, T.sg, acc);
       else epi_chunk_ip<KT, NCH, NR>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
     } else {
       epi_chunk_ip<KT, NCH, NR>(h, l, bm, c0, ncols - c0, rc, T.kp, acc);
@@ -2306,11 +2412,12 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   const size_t o_xbf = o_xaf + (ff ? al((size_t)ffa * k * sizeof(float2)) : 0);
   // anchored polynomial: source mean and weight sum (ybar | wsum | block
   // partials) and the rows' v0^p
-  const bool anch = ker->type == KS_POLYNOMIAL && ker->powe == rint(ker->powe) && ker->powe >= 1.0 &&
-                    ker->powe <= 4.0;
+  const bool anch = ker->type == KS_TANH || ker->type == KS_QUARTIC || ker->type == KS_EPANECHNIKOV ||
+                    ker->type == KS_MULTIQUADRATIC ||
+                    (ker->type == KS_POLYNOMIAL && ker->powe == rint(ker->powe) && ker->powe >= 1.0 && ker->powe <= 4.0);
   const int nwb = (n + ANCHOR_WPER - 1) / ANCHOR_WPER;   // blocks of the weight sum
   const size_t o_anc = o_xbf + (ff ? al((size_t)ffb * k * sizeof(float2)) : 0);
-  const size_t o_rowc = o_anc + (anch ? al(((size_t)k + RMAX + (size_t)nwb * nrhs) * 8) : 0);
+  const size_t o_rowc = o_anc + (anch ? al(((size_t)2 * k + RMAX + (size_t)nwb * nrhs) * 8) : 0);
   const size_t total = o_rowc + (anch ? al((size_t)m * 8) : 0);
   uint8_t *ws = nullptr;
   if (stream_ordered_alloc) {
@@ -2338,14 +2445,15 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   }
   params_kernel<<<1, 1024, 0, s>>>(k, ker->type, ker->scal, ker->cons, ker->powe, tau, bbox, centre, P);
   double *ybar = anch ? (double *)(ws + o_anc) : nullptr;
+  double *ybsq = anch ? ybar + k + RMAX + (size_t)nwb * nrhs : nullptr;   // after the weight-sum partials
   double *rowc = anch ? (double *)(ws + o_rowc) : nullptr;
   if (anch) {   // ybar[k] | wsum[RMAX] | the weight-sum blocks' partials
     anchor_partial<<<(k + 31) / 32 + nwb, 256, 0, s>>>(n, k, XB, bmap, nxb, w, wmap, nrhs, err_word(c), ybar,
-                                                      ybar + k + RMAX);
+                                                      ybar + k + RMAX, ybsq);
     anchor_final<<<1, 32, 0, s>>>(nwb, nrhs, ybar + k + RMAX, ybar + k);
   }
   pack_kernel<<<ntm, BM, 0, s>>>(0, m, k, kpad, XA, amap, nxa, err_word(c), nullptr, nullptr, hi, ker->type,
-                                 centre, P, ws + o_a, nullptr, nullptr, nullptr, ybar, rowc);
+                                 centre, P, ws + o_a, nullptr, nullptr, nullptr, ybar, rowc, 1, ybsq);
   pack_kernel<<<ntn, BN, 0, s>>>(1, n, k, kpad, XB, bmap, nxb, err_word(c), w, wmap, hj, ker->type, centre,
                                  P, ws + o_b, nullptr, nullptr, nullptr, nullptr, nullptr, nrhs);
 
@@ -2619,7 +2727,8 @@ int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, con
   // rows' v0^p
   Pl.any_anch = false;
   for (int t = 0; t < ntask && !Pl.any_anch; t++)
-    Pl.any_anch = kps[t].type == KS_POLYNOMIAL && kps[t].pmode == POW_INT && kps[t].pint >= 1 && kps[t].pint <= 4;
+    Pl.any_anch = (kps[t].type == KS_POLYNOMIAL && kps[t].pmode == POW_INT && kps[t].pint >= 1 && kps[t].pint <= 4) ||
+                  kps[t].type == KS_TANH;
   Pl.o_ybar = Pl.o_xbf + (same_pool ? 0 : al((size_t)nxb * k * sizeof(float2)));
   Pl.o_wsum = Pl.o_ybar + (Pl.any_anch ? al((size_t)ntask * k * 8) : 0);
   Pl.o_rowc = Pl.o_wsum + (Pl.any_anch ? al((size_t)ntask * 8) : 0);

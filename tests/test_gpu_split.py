@@ -115,6 +115,24 @@ def test_split_polynomial_on_a_constant(gpu, oracle_mod, pw):
     assert e["normwise"] <= 5e-7 and e["cond_max"] <= 1e-8, e
 
 
+def test_split_tanh_on_a_constant(gpu, oracle_mod):
+    """tanh(x.y/64 + 0.2) on uniform [0, 1]^64 with weights of zero sum: the
+    values sit within a few percent of tanh(0.45); summed around per-row
+    anchors (addition theorem near the anchor)."""
+    X, w, amap, bmap, umap, wmap = _case(14, 12000, 64, 2500, 6000)
+    w[wmap] -= w[wmap].mean()
+    e = _run(gpu, oracle_mod, 4, dict(scal=1 / 64, cons=0.2), X, w, amap, bmap, umap, wmap)
+    assert e["normwise"] <= 5e-7 and e["cond_max"] <= 1e-8, e
+
+
+def test_split_tanh_saturating(gpu, oracle_mod):
+    """tanh(x.y) on N(0, 1) points in k = 16: values across both saturated
+    ends, far from the rows' anchors (evaluated directly there)."""
+    X, w, amap, bmap, umap, wmap = _case(15, 4000, 16, 800, 1000, dist="normal")
+    e = _run(gpu, oracle_mod, 4, dict(scal=1.0, cons=0.0), X, w, amap, bmap, umap, wmap)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
+
+
 def _mixture(seed, N, k, ncl=64, sigma=0.05, dup=0.01):
     rng = np.random.default_rng(seed)
     centres = rng.uniform(-10, 10, (ncl, k))
