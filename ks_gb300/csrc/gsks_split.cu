@@ -558,55 +558,55 @@ __device__ void block_source_sums(int j0, int j1, int k, const double *__restric
 
 // Anchor point of a single call's polynomial, tanh and compact / multiquadratic
 // kernels (the sources' mean and mean squares per coordinate) and the sum of
-// all weights.  Any point inside the sources' hull keeps each row's anchor value
-// within the range of that row's values, so the mean of a strided sample of
-// at most ANCHOR_SAMPLE sources serves (blocks 0 .. ceil(k/32)-1: 32
-// coordinates each, 8 warps over the sample, combined in warp order).  The
-// weight sum covers every source (blocks from ceil(k/32) on: contiguous
-// ranges, fixed-order tree; anchor_final adds the ranges in order).  All of
-// it deterministic.
+// all weights.  Any point inside the sources' hull keeps each row's anchor
+// value within the range of that row's values, so the mean of a strided
+// sample of at most ANCHOR_SAMPLE sources serves: anchor_coords blocks (cb,
+// sb) take 32 coordinates of ANCHOR_SB-th of the sample each.  The weight sum
+// covers every source (anchor_weights: contiguous ranges, fixed-order tree).
+// anchor_final adds the partials in order.  All of it deterministic.
 constexpr int ANCHOR_SAMPLE = 2048;
+constexpr int ANCHOR_SB = 16;       // sample blocks of anchor_coords
 constexpr int ANCHOR_WPER = 4096;   // weights per block of the weight sum
 
-__global__ void __launch_bounds__(256) anchor_partial(int n, int k, const double *__restrict__ XB,
-                                                      const int *__restrict__ bmap, int nxb,
-                                                      const double *__restrict__ w, const int *__restrict__ wmap,
-                                                      int nrhs, int *err, double *__restrict__ ybar,
-                                                      double *__restrict__ wpart, double *__restrict__ ybsq)
+// cpart[(sb * 2 + 0) * k + p]: sum of coordinate p over sample block sb;
+// cpart[(sb * 2 + 1) * k + p]: the sum of its squares.
+__global__ void __launch_bounds__(256) anchor_coords(int n, int k, const double *__restrict__ XB,
+                                                     const int *__restrict__ bmap, int nxb, int *err,
+                                                     double *__restrict__ cpart)
 {
-  // nrhs interleaved weight columns: one sum per column (wpart[b nrhs + r])
-  __shared__ double sh[256];
-  const int ncb = (k + 31) / 32, t = threadIdx.x, lane = t & 31, wp = t >> 5;
-  if ((int)blockIdx.x < ncb) {
-    const int S = min(n, ANCHOR_SAMPLE), stride = n / S;
-    const int p = blockIdx.x * 32 + lane;
-    double s = 0.0, s2 = 0.0;
-    if (p < k) {
-#pragma unroll 4
-      for (int q = wp; q < S; q += 8) {
-        const double y = XB[(size_t)pool_index(bmap, q * stride, nxb, err) * k + p];
-        s += y;
-        s2 = fma(y, y, s2);
-      }
+  __shared__ double sh[2][256];
+  const int t = threadIdx.x, lane = t & 31, wp = t >> 5;
+  const int S = min(n, ANCHOR_SAMPLE), stride = n / S;
+  const int per = (S + ANCHOR_SB - 1) / ANCHOR_SB;
+  const int q0 = blockIdx.y * per, q1 = min(S, q0 + per);
+  const int p = blockIdx.x * 32 + lane;
+  double s = 0.0, s2 = 0.0;
+  if (p < k) {
+#pragma unroll 8
+    for (int q = q0 + wp; q < q1; q += 8) {
+      const double y = XB[(size_t)pool_index(bmap, q * stride, nxb, err) * k + p];
+      s += y;
+      s2 = fma(y, y, s2);
     }
-    sh[t] = s;
-    __syncthreads();
-    if (wp == 0 && p < k) {
-      double r = 0.0;
-      for (int q = 0; q < 8; q++) r += sh[q * 32 + lane];
-      ybar[p] = r / (double)S;
-    }
-    __syncthreads();
-    sh[t] = s2;
-    __syncthreads();
-    if (wp == 0 && p < k) {   // the sample's mean square of coordinate p (distance kernels' anchors)
-      double r = 0.0;
-      for (int q = 0; q < 8; q++) r += sh[q * 32 + lane];
-      ybsq[p] = r / (double)S;
-    }
-    return;
   }
-  const int b = blockIdx.x - ncb;
+  sh[0][t] = s;
+  sh[1][t] = s2;
+  __syncthreads();
+  if (wp == 0 && p < k) {
+    double r = 0.0, r2 = 0.0;
+    for (int q = 0; q < 8; q++) { r += sh[0][q * 32 + lane]; r2 += sh[1][q * 32 + lane]; }
+    cpart[((size_t)blockIdx.y * 2 + 0) * k + p] = r;
+    cpart[((size_t)blockIdx.y * 2 + 1) * k + p] = r2;
+  }
+}
+
+// wpart[b * nrhs + r]: the sum of weight column r over sources b ANCHOR_WPER ..
+__global__ void __launch_bounds__(256) anchor_weights(int n, const double *__restrict__ w,
+                                                      const int *__restrict__ wmap, int nrhs,
+                                                      double *__restrict__ wpart)
+{
+  __shared__ double sh[256];
+  const int t = threadIdx.x, b = blockIdx.x;
   const int j0 = b * ANCHOR_WPER, j1 = min(n, j0 + ANCHOR_WPER);
   for (int r = 0; r < nrhs; r++) {
     double s = 0.0;
@@ -622,13 +622,26 @@ __global__ void __launch_bounds__(256) anchor_partial(int n, int k, const double
   }
 }
 
-__global__ void anchor_final(int nwb, int nrhs, const double *__restrict__ wpart, double *__restrict__ wsum)
+// ybar[p], ybsq[p]: the sample's mean and mean square of coordinate p;
+// wsum[r]: the sum of weight column r.
+__global__ void anchor_final(int n, int k, int nwb, int nrhs, const double *__restrict__ cpart,
+                             const double *__restrict__ wpart, double *__restrict__ ybar,
+                             double *__restrict__ ybsq, double *__restrict__ wsum)
 {
-  const int r = threadIdx.x;
-  if (blockIdx.x == 0 && r < nrhs) {
-    double s = 0.0;
-    for (int b = 0; b < nwb; b++) s += wpart[(size_t)b * nrhs + r];
-    wsum[r] = s;
+  const double inv = 1.0 / (double)min(n, ANCHOR_SAMPLE);
+  for (int p = threadIdx.x; p < k; p += blockDim.x) {
+    double a = 0.0, b = 0.0;
+    for (int sb = 0; sb < ANCHOR_SB; sb++) {
+      a += cpart[((size_t)sb * 2 + 0) * k + p];
+      b += cpart[((size_t)sb * 2 + 1) * k + p];
+    }
+    ybar[p] = a * inv;
+    ybsq[p] = b * inv;
+  }
+  for (int r = threadIdx.x; r < nrhs; r += blockDim.x) {
+    double a = 0.0;
+    for (int b = 0; b < nwb; b++) a += wpart[(size_t)b * nrhs + r];
+    wsum[r] = a;
   }
 }
 
@@ -2417,7 +2430,9 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
                     (ker->type == KS_POLYNOMIAL && ker->powe == rint(ker->powe) && ker->powe >= 1.0 && ker->powe <= 4.0);
   const int nwb = (n + ANCHOR_WPER - 1) / ANCHOR_WPER;   // blocks of the weight sum
   const size_t o_anc = o_xbf + (ff ? al((size_t)ffb * k * sizeof(float2)) : 0);
-  const size_t o_rowc = o_anc + (anch ? al(((size_t)2 * k + RMAX + (size_t)nwb * nrhs) * 8) : 0);
+  // ybar[k] | wsum[RMAX] | wpart[nwb nrhs] | ybsq[k] | cpart[ANCHOR_SB 2 k]
+  const size_t o_rowc = o_anc + (anch ? al(((size_t)2 * k + RMAX + (size_t)nwb * nrhs +
+                                            (size_t)ANCHOR_SB * 2 * k) * 8) : 0);
   const size_t total = o_rowc + (anch ? al((size_t)m * 8) : 0);
   uint8_t *ws = nullptr;
   if (stream_ordered_alloc) {
@@ -2447,10 +2462,11 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
   double *ybar = anch ? (double *)(ws + o_anc) : nullptr;
   double *ybsq = anch ? ybar + k + RMAX + (size_t)nwb * nrhs : nullptr;   // after the weight-sum partials
   double *rowc = anch ? (double *)(ws + o_rowc) : nullptr;
-  if (anch) {   // ybar[k] | wsum[RMAX] | the weight-sum blocks' partials
-    anchor_partial<<<(k + 31) / 32 + nwb, 256, 0, s>>>(n, k, XB, bmap, nxb, w, wmap, nrhs, err_word(c), ybar,
-                                                      ybar + k + RMAX, ybsq);
-    anchor_final<<<1, 32, 0, s>>>(nwb, nrhs, ybar + k + RMAX, ybar + k);
+  if (anch) {
+    double *wpart = ybar + k + RMAX, *cpart = ybsq + k;
+    anchor_coords<<<dim3((k + 31) / 32, ANCHOR_SB), 256, 0, s>>>(n, k, XB, bmap, nxb, err_word(c), cpart);
+    anchor_weights<<<nwb, 256, 0, s>>>(n, w, wmap, nrhs, wpart);
+    anchor_final<<<1, 256, 0, s>>>(n, k, nwb, nrhs, cpart, wpart, ybar, ybsq, ybar + k);
   }
   pack_kernel<<<ntm, BM, 0, s>>>(0, m, k, kpad, XA, amap, nxa, err_word(c), nullptr, nullptr, hi, ker->type,
                                  centre, P, ws + o_a, nullptr, nullptr, nullptr, ybar, rowc, 1, ybsq);
@@ -2514,7 +2530,7 @@ int enqueue_split(Ctx *c, const ks_t *ker, int m, int n, int k, double *u, const
     e = launch_rescue(a, std::max(1, std::min(2 * sms, (m + 7) / 8)), rlist, rcount, u, umap, s, NRK);
   if (stream_ordered_alloc) cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_status(e, "split launch");
-  note_launches((defer ? 8 : 7) + ff_launches + (anch ? 2 : 0));
+  note_launches((defer ? 8 : 7) + ff_launches + (anch ? 3 : 0));
   return GSKS_OK;
 }
 
