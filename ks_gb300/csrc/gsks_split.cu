@@ -133,6 +133,7 @@ struct Params {          // per call, computed on the device
   float rc;              // -g as a float
   float t_flag;          // flag pairs with t < t_flag ...
   float rho;             // ... or t < rho * (n_i + n_j)
+  float nbmax;           // bound of every |x''|^2 (scaled units): n_j <= nbmax
   int centred;
   int any_flag;          // some pair may be flagged
   int exact_t1;          // nu_i + nu_j - H is exact in FP32
@@ -177,7 +178,7 @@ struct __align__(16) TaskParam {
   int gfast;             // Gaussian without flags: low norm parts folded (as Params::gfast)
   int anch;              // polynomial of power 1..4 summed around row anchors (as Params::anch)
   float sg;              // scal * g / 2 (anch)
-  int pad;
+  float nbmax;           // bound of every point's |x''|^2 at the task's scale (the flag test)
 };
 static_assert(sizeof(TaskParam) % 16 == 0, "TaskParam is copied by the bulk-copy engine");
 
@@ -425,6 +426,7 @@ __global__ void params_kernel(int k, int kt, double scal, double cons, double po
       rho = 0.0f;                             // compact / polynomial in d2: absolute error only
     }
     P->t_flag = t_flag; P->rho = rho;
+    P->nbmax = (float)(nbound * (1.0 + 0x1p-20));
     P->any_flag = (t_flag > 0.0f || rho > 0.0f) ? 1 : 0;
     // |x''|^2 + |y''|^2 lies on the grid q and -2 sigma^2 2^-14 H on the grid
     // 2 sigma^2 2^-14; when the latter is a multiple of q their sum is exact
@@ -479,7 +481,7 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   T.anch = ((kp.type == KS_POLYNOMIAL && kp.pmode == POW_INT && kp.pint >= 1 && kp.pint <= 4) ||
             kp.type == KS_TANH) ? 1 : 0;
   T.sg = (float)(kp.scal * 0.5 * g);
-  T.pad = 0;
+  T.nbmax = (float)(nbound * (1.0 + 0x1p-20));
   if (kp.type == KS_GAUSSIAN) {
     T.s2 = (float)s2;                      // the rechecks work from the pool coordinates
     T.s2l = (float)(s2 - (double)T.s2);
@@ -1516,8 +1518,11 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
 {
   const KParams &kp = T.kp;
   uint32_t flags = 0;
-  float t_flag = 0.f, rho = 0.f;
-  if constexpr (FLAGS) { t_flag = T.t_flag; rho = T.rho; }
+  // flag test: t < t_flag or t < rho (n_i + n_j), tested against the row's
+  // bound max(t_flag, rho (n_i + nbmax)) (a superset: the extra pairs are
+  // rechecked exactly), one comparison per column
+  float t_flag = 0.f;
+  if constexpr (FLAGS) t_flag = fmaxf(T.t_flag, T.rho * fmaf(am.n_hi, -rc, T.nbmax));
   const uint64_t AN = pk2(am.n_hi, am.n_hi), ANL = pk2(am.n_lo, am.n_lo), NRC = pk2(-rc, -rc);
 #pragma unroll
   for (int j4 = 0; j4 < NC; j4 += 4) {
@@ -1584,7 +1589,7 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
           const float f = -am.h * f4(hh, q);      // 0.5 log2(e) h_i h_j
           if (f > t_flag && t * f < 126.f) { flags |= 1u << j; kv = 0.f; }
         } else {
-          if (t < fmaxf(t_flag, rho * s)) { flags |= 1u << j; kv = 0.f; }
+          if (t < t_flag) { flags |= 1u << j; kv = 0.f; }
         }
       }
       // padding columns carry w = 0 and finite distances
@@ -2082,7 +2087,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     TaskParam T0;                                  // the single call's parameters
     if constexpr (KT != KS_LIST) {
       const double s2 = a.kp.scal * 1.4426950408889634;   // Gaussian rechecks from pool coordinates
-      T0.kp = a.kp; T0.t_flag = P->t_flag; T0.rho = P->rho;
+      T0.kp = a.kp; T0.t_flag = P->t_flag; T0.rho = P->rho; T0.nbmax = P->nbmax;
       T0.s2 = (float)s2; T0.s2l = (float)(s2 - (double)T0.s2);
       T0.lap = P->lap; T0.any_flag = P->any_flag; T0.centred = P->centred;
       T0.anch = P->anch; T0.sg = P->sg;
