@@ -467,6 +467,7 @@ int dgsks_status(ks_t *kernel, int m, int n, int k,
                  double *XB, double *XB2, int *bmap,
                  double *w, int *wmap)
 {
+  NvtxRange nvtx_("dgsks");
   tl_launches = 0;
   if (m < 0 || n < 0 || k < 0) return set_status(GSKS_ERR_ARG, "dgsks");
   // early return before the kernel-type switch, as frame/dgsks.c:394-397
@@ -515,6 +516,7 @@ int gsks_dgsks_device(ks_t *kernel, int m, int n, int k,
                       const double *w, const int *wmap,
                       int precision, void *stream)
 {
+  NvtxRange nvtx_("gsks_dgsks_device");
   tl_launches = 0;
   if (m < 0 || n < 0 || k < 0) return set_status(GSKS_ERR_ARG, "gsks_dgsks_device");
   if (m == 0 || n == 0 || k == 0) return set_status(GSKS_OK, nullptr);
@@ -537,6 +539,7 @@ int gsks_dgsks_device_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
                           const double *w, const int *wmap,
                           int precision, void *stream)
 {
+  NvtxRange nvtx_("gsks_dgsks_device_rhs");
   tl_launches = 0;
   if (m < 0 || n < 0 || k < 0 || nrhs < 1) return set_status(GSKS_ERR_ARG, "gsks_dgsks_device_rhs");
   if (m == 0 || n == 0 || k == 0) return set_status(GSKS_OK, nullptr);
@@ -558,6 +561,7 @@ int dgsks_rhs(ks_t *kernel, int m, int n, int k, int nrhs,
               double *XB, double *XB2, int *bmap,
               double *w, int *wmap)
 {
+  NvtxRange nvtx_("dgsks_rhs");
   tl_launches = 0;
   if (m < 0 || n < 0 || k < 0 || nrhs < 1) return set_status(GSKS_ERR_ARG, "dgsks_rhs");
   if (m == 0 || n == 0 || k == 0) return set_status(GSKS_OK, nullptr);

@@ -5,8 +5,19 @@
 #include <cuda_runtime.h>
 #include "ks.h"
 #include "gsks_internal.cuh"
+#include <nvtx3/nvToolsExt.h>
 
 namespace gsks {
+
+// A named NVTX range around an entry point, for timeline profilers (Nsight
+// Systems, ncu's NVTX filters); a push and a pop of a few nanoseconds when no
+// tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Growable device / pinned host buffers owned by a per-thread context.
 struct DevBuf {
@@ -116,6 +127,7 @@ struct SplitListPlan {
   // weight sums, the rows' v0^p
   bool any_anch = false;
   size_t o_ybar = 0, o_wsum = 0, o_rowc = 0;
+  size_t o_tbox = 0, o_tcen = 0;   // per-task boxes and centres (each task's own frame)
 };
 int split_list_plan(SplitListPlan &P, const KParams *kps, int ntask, int k, const int *hoff_a, const int *hoff_b,
                     const long long *pbase, int chunk, int nxa, int nxb, bool same_pool, cudaStream_t s);

@@ -367,6 +367,7 @@ extern "C" int dgsks_list(ks_t *kernel, ks_t *kernels, int ntask, int k,
                           double *XB, double *XB2, int nxb,
                           double *w, int nw)
 {
+  NvtxRange nvtx_("dgsks_list");
   note_launches(0);
   if (ntask < 0 || k < 0 || nu < 0 || nxa < 0 || nxb < 0 || nw < 0)
     return set_status(GSKS_ERR_ARG, "dgsks_list");
@@ -462,6 +463,7 @@ extern "C" int gsks_list_plan_create(gsks_list_plan **out, ks_t *kernel, ks_t *k
 extern "C" int gsks_list_plan_execute(gsks_list_plan *p, double *u, const double *XA, const double *XA2,
                                       const double *XB, const double *XB2, const double *w, void *stream)
 {
+  NvtxRange nvtx_("gsks_list_plan_execute");
   if (!p || !u || !XA || !XB || !w) return set_status(GSKS_ERR_ARG, "gsks_list_plan_execute");
   Ctx *c = get_ctx();
   if (!c) return gsks_last_error();

@@ -129,6 +129,7 @@ extern "C" void dgsks_ref(ks_t *kernel, int m, int n, int k,
                           double *XB, double *XB2, int *bmap,
                           double *w, int *wmap)
 {
+  NvtxRange nvtx_("dgsks_ref");
   note_launches(0);
   if (m < 0 || n < 0 || k < 0) { set_status(GSKS_ERR_ARG, "dgsks_ref"); return; }
   if (m == 0 || n == 0 || k == 0) { set_status(GSKS_OK, nullptr); return; }

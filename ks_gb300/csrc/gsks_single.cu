@@ -67,6 +67,7 @@ int sgsks_status(ks_t *kernel, int m, int n, int k,
                  float *XB, float *XB2, int *bmap,
                  float *w, int *wmap)
 {
+  NvtxRange nvtx_("sgsks");
   (void)XA2; (void)XB2;   // recomputed in FP64 from the converted coordinates
   if (m < 0 || n < 0 || k < 0) return set_status(GSKS_ERR_ARG, "sgsks");
   if (m == 0 || n == 0 || k == 0) return set_status(GSKS_OK, nullptr);

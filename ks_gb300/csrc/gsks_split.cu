@@ -444,13 +444,68 @@ __global__ void params_kernel(int k, int kt, double scal, double cons, double po
 
 }
 
+// Per task of the list form, the per-dimension min and max (ordered keys)
+// over its targets (XA through a_idx) and sources (XB through b_idx):
+// tbox[t][0][p], tbox[t][1][p]; each task's box is also folded into the
+// global one (bbox, from bbox_init) with one atomic per dimension and bound.
+// One block per task, the threads over (dimension, stride of points).
+__global__ void __launch_bounds__(256) list_box_kernel(int ntask, int k, const SplitTaskGeo *__restrict__ tg,
+                                                       const double *__restrict__ XA, const int *__restrict__ a_idx,
+                                                       int nxa, const double *__restrict__ XB,
+                                                       const int *__restrict__ b_idx, int nxb, int *err,
+                                                       long long *__restrict__ tbox, long long *__restrict__ bbox)
+{
+  __shared__ long long slo[256], shi[256];
+  const int t = blockIdx.x;
+  if (t >= ntask) return;
+  const SplitTaskGeo G = tg[t];
+  const int npts = G.m + G.n, tid = threadIdx.x;
+  for (int p0 = 0; p0 < k; p0 += blockDim.x) {
+    const int cols = min((int)blockDim.x, k - p0);
+    const int sub = blockDim.x / cols;
+    const int c = tid % cols, grp = tid / cols;
+    long long lo = 0x7FFFFFFFFFFFFFFFLL, hi = (long long)0x8000000000000000ULL;
+    if (grp < sub) {
+      const int p = p0 + c;
+      for (int q = grp; q < npts; q += sub) {
+        const double v = q < G.m ? XA[(size_t)pool_index(a_idx, G.a0 + q, nxa, err) * k + p]
+                                 : XB[(size_t)pool_index(b_idx, G.b0 + q - G.m, nxb, err) * k + p];
+        const long long key = dkey(v);
+        lo = min(lo, key);
+        hi = max(hi, key);
+      }
+    }
+    slo[tid] = lo;
+    shi[tid] = hi;
+    __syncthreads();
+    if (tid < cols) {
+      for (int q = 1; q < sub; q++) { lo = min(lo, slo[q * cols + tid]); hi = max(hi, shi[q * cols + tid]); }
+      tbox[(size_t)t * 2 * k + p0 + tid] = lo;
+      tbox[(size_t)t * 2 * k + k + p0 + tid] = hi;
+      if (npts > 0) {
+        atomicMin(&bbox[p0 + tid], lo);
+        atomicMax(&bbox[k + p0 + tid], hi);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Per-task parameters of the list form: the scale of the task's tile images
 // and the flag thresholds, by the rules of params_kernel with the task's own
 // kernel.  Distance tasks take the centred box, inner-product tasks the
 // uncentred one; Gaussian tasks fold their bandwidth into the coordinates
 // (scaled units, as a single call), the others keep them unscaled.
+//
+// Every task takes its own box (tbox: ordered keys of the per-dimension min
+// and max over the task's targets and sources, list_box_kernel): distance
+// tasks are centred on the box's centre (tcen[t k + p], written here), and
+// the scale follows the task's own extent, so that spatially local tasks (a
+// tree code's near-field blocks) keep a small distance error bound however
+// far they lie from the other tasks.
 __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, const Params *__restrict__ P,
-                                   float tau, TaskParam *__restrict__ out)
+                                   float tau, TaskParam *__restrict__ out, const long long *__restrict__ tbox,
+                                   double *__restrict__ tcen)
 {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntask) return;
@@ -458,10 +513,23 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
   const bool centred = kt_uses_norms(kp.type);
   const double s2 = kp.scal * 1.4426950408889634;
   const double alpha = kp.type == KS_GAUSSIAN ? sqrt(fmax(-s2, 0.0)) : 1.0;
-  const double maxabs = alpha * (centred ? P->mx_c : P->mx_u);
+  double mx_c = 0.0, sq_c = 0.0, mx_u = 0.0, sq_u = 0.0;
+  {
+    const int k = P->k;
+    const long long *lo = tbox + (size_t)t * 2 * k, *hi = lo + k;
+    const bool empty = lo[0] > hi[0];   // a task without points (no items either)
+    for (int p = 0; p < k; p++) {
+      const double a = empty ? 0.0 : dval(lo[p]), b = empty ? 0.0 : dval(hi[p]);
+      const double hc = 0.5 * (b - a), hu = fmax(fabs(a), fabs(b));
+      tcen[(size_t)t * k + p] = 0.5 * (a + b);
+      mx_c = fmax(mx_c, hc); sq_c += hc * hc;
+      mx_u = fmax(mx_u, hu); sq_u += hu * hu;
+    }
+  }
+  const double maxabs = alpha * (centred ? mx_c : mx_u);
   double sigma = maxabs > 0.0 ? exp2(ceil(log2(maxabs))) : 1.0;
   if (sigma < maxabs) sigma *= 2.0;
-  const double nbound = alpha * alpha * (centred ? P->sq_c : P->sq_u);
+  const double nbound = alpha * alpha * (centred ? sq_c : sq_u);
   const double q = exp2(ceil(log2(2.0 * nbound + 1e-300)) - 23.0);
   const double g = 2.0 * sigma * sigma * 0x1p-14;
   const int k = P->k;
@@ -693,6 +761,8 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
   }
   const int pidx = valid ? pool_index(map, pt, npool, err) : 0;
   const double *x = X + (size_t)pidx * k;
+  // the centre: the call's, or (list form) the task's own (centre + task k)
+  const double *cen = tiles ? centre + (size_t)tile_task[tile] * k : centre;
   // coordinate -> slice units: the call's scale, or the list task's
   const TaskParam *TT = tiles ? &tp[tile_task[tile]] : nullptr;
   const double sc = TT ? TT->sc : P->alpha * P->inv_sigma * 128.0;
@@ -716,7 +786,7 @@ __global__ void pack_kernel(int side, int npts, int k, int kpad, const double *_
       float a1 = 0.0f;
       __half h2 = __float2half_rn(0.0f), h3 = __float2half_rn(0.0f);
       if (valid && p < k) {
-        const double t = (centred ? x[p] - centre[p] : x[p]) * sc;   // the difference is exact near the centre
+        const double t = (centred ? x[p] - cen[p] : x[p]) * sc;   // the difference is exact near the centre
         a1 = rintf((float)t);                          // |a1| <= 128
         const float r1 = (float)(t - (double)a1);      // |r1| <= 1/2 (+ a rounding at ties)
         h2 = __float2half_rn(r1);
@@ -2753,7 +2823,10 @@ int split_list_plan(SplitListPlan &Pl, const KParams *kps, int ntask, int k, con
   Pl.o_ybar = Pl.o_xbf + (same_pool ? 0 : al((size_t)nxb * k * sizeof(float2)));
   Pl.o_wsum = Pl.o_ybar + (Pl.any_anch ? al((size_t)ntask * k * 8) : 0);
   Pl.o_rowc = Pl.o_wsum + (Pl.any_anch ? al((size_t)ntask * 8) : 0);
-  const size_t total = Pl.o_rowc + (Pl.any_anch ? al((size_t)std::max(Pl.ma, 1) * 8) : 0);
+  // per-task boxes (2 k keys) and centres (k doubles)
+  Pl.o_tbox = Pl.o_rowc + (Pl.any_anch ? al((size_t)std::max(Pl.ma, 1) * 8) : 0);
+  Pl.o_tcen = Pl.o_tbox + al((size_t)ntask * 2 * k * sizeof(long long));
+  const size_t total = Pl.o_tcen + al((size_t)ntask * k * sizeof(double));
   if (!Pl.ws.ensure(total)) return GSKS_ERR_ALLOC;
   uint8_t *ws = (uint8_t *)Pl.ws.p;
   auto up = [&](size_t off, const void *src, size_t bytes) {
@@ -2788,28 +2861,25 @@ int split_list_run(const SplitListPlan &Pl, Ctx *c, const double *XA, const int 
   TaskParam *tp = (TaskParam *)(ws + Pl.o_tp);
   const float tau = 5e-7f;
   const int sms = std::max(1, c->num_sms);
-  bbox_init<<<1, 256, 0, s>>>(k, bbox);
-  {
-    // every list position (tasks with an empty side included: harmless)
-    const long long tot = ((long long)Pl.ma + Pl.mb) * k;
-    const int blocks = (int)std::max<long long>((k + 255) / 256,
-                                                std::min<long long>(8LL * sms, std::max<long long>(1, (tot + 255) / 256)));
-    bbox_kernel<<<blocks, 256, 2 * k * sizeof(long long), s>>>(Pl.ma, Pl.mb, k, XA, a_idx, nxa, XB, b_idx, nxb, err,
-                                                               bbox);
-  }
-  params_kernel<<<1, 1024, 0, s>>>(k, KS_LIST, 0.0, 0.0, 0.0, tau, bbox, centre, P);
-  task_params_kernel<<<(ntask + 127) / 128, 128, 0, s>>>(ntask, (const KParams *)(ws + Pl.o_kps), P, tau, tp);
   const SplitTaskGeo *tg = (const SplitTaskGeo *)(ws + Pl.o_tg);
+  long long *tbox = (long long *)(ws + Pl.o_tbox);
+  double *tcen = (double *)(ws + Pl.o_tcen);
+  bbox_init<<<1, 256, 0, s>>>(k, bbox);
+  // every task's box (its targets and sources), folded into the global box
+  list_box_kernel<<<ntask, 256, 0, s>>>(ntask, k, tg, XA, a_idx, nxa, XB, b_idx, nxb, err, tbox, bbox);
+  params_kernel<<<1, 1024, 0, s>>>(k, KS_LIST, 0.0, 0.0, 0.0, tau, bbox, centre, P);
+  task_params_kernel<<<(ntask + 127) / 128, 128, 0, s>>>(ntask, (const KParams *)(ws + Pl.o_kps), P, tau, tp, tbox,
+                                                          tcen);
   double *ybar = Pl.any_anch ? (double *)(ws + Pl.o_ybar) : nullptr;
   double *wsum = Pl.any_anch ? (double *)(ws + Pl.o_wsum) : nullptr;
   double *rowc = Pl.any_anch ? (double *)(ws + Pl.o_rowc) : nullptr;
   if (Pl.any_anch)
     list_anchor<<<ntask, 256, 256 * sizeof(double), s>>>(ntask, k, tp, tg, XB, b_idx, nxb, w, w_idx, err, ybar, wsum);
   pack_kernel<<<Pl.n_ta, BM, 0, s>>>(0, 0, k, kpad, XA, a_idx, nxa, err, nullptr, nullptr, nullptr, KS_LIST,
-                                     centre, P, ws + Pl.o_a, (const int2 *)(ws + Pl.o_ta),
+                                     tcen, P, ws + Pl.o_a, (const int2 *)(ws + Pl.o_ta),
                                      (const int *)(ws + Pl.o_tat), tp, ybar, rowc);
   pack_kernel<<<Pl.n_tb, BN, 0, s>>>(1, 0, k, kpad, XB, b_idx, nxb, err, w, w_idx, nullptr, KS_LIST,
-                                     centre, P, ws + Pl.o_b, (const int2 *)(ws + Pl.o_tb),
+                                     tcen, P, ws + Pl.o_b, (const int2 *)(ws + Pl.o_tb),
                                      (const int *)(ws + Pl.o_tbt), tp, nullptr, nullptr);
   float2 *xaf = (float2 *)(ws + Pl.o_xaf), *xbf = Pl.same_pool ? xaf : (float2 *)(ws + Pl.o_xbf);
   {

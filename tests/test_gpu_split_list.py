@@ -212,3 +212,29 @@ def test_split_list_polynomial_on_a_constant(gpu, oracle_mod):
     specs = [(1, dict(scal=1.0 / k, cons=1.0, powe=float(1 + t % 4))) for t in range(ntask)]
     _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True)
     assert e["normwise"] <= 5e-7 and e["cond_max"] <= 1e-8, e
+
+
+def test_split_list_local_tasks_far_apart(gpu, oracle_mod):
+    """Tree-code-like lists: every task's targets and sources come from one
+    small cluster (sigma 0.05) of a mixture spread over [-10, 10]^32.  Each
+    task is centred and scaled on its own box, so narrow Gaussians and the
+    Laplace kernel resolve within the cluster without the error bound of the
+    whole data set."""
+    O = oracle_mod
+    rng = np.random.default_rng(51)
+    k, ncl, per = 32, 24, 1200
+    centres = rng.uniform(-10, 10, (ncl, k))
+    X = (centres[:, None, :] + 0.05 * rng.standard_normal((ncl, per, k))).reshape(-1, k)
+    N = X.shape[0]
+    w = rng.standard_normal(N)
+    sa = rng.integers(200, 800, ncl); sb = rng.integers(300, 900, ncl)
+    a_idx = np.concatenate([c * per + rng.permutation(per)[:sa[c]] for c in range(ncl)]).astype(np.int32)
+    b_idx = np.concatenate([c * per + rng.permutation(per)[:sb[c]] for c in range(ncl)]).astype(np.int32)
+    a_off = np.concatenate([[0], np.cumsum(sa)]).astype(np.int32)
+    b_off = np.concatenate([[0], np.cumsum(sb)]).astype(np.int32)
+    u_idx = a_idx.copy(); w_idx = b_idx.copy()
+    specs = []
+    for t in range(ncl):
+        specs.append([(0, dict(scal=-12.5)), (2, {}), (0, dict(scal=-200.0))][t % 3])
+    _, e = _run_list(gpu, O, specs, X, w, a_off, a_idx, u_idx, b_off, b_idx, w_idx, device=True)
+    assert e["normwise"] <= TOL and e["cond_max"] <= TOL, e
