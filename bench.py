@@ -448,6 +448,9 @@ def run_ours(args, ws, rank, local):
         del wl
         torch.cuda.empty_cache()
         line["list"] = run_list(args, torch, gsks, forms)
+    if not args.no_list and ws == 1:
+        torch.cuda.empty_cache()
+        line["list_local"] = run_list_local(args, torch, gsks)
     if not args.no_configs and ws == 1:
         torch.cuda.empty_cache()
         line["configs"] = run_configs_default(args, torch, gsks)
@@ -525,6 +528,44 @@ def run_rhs(args, torch, gsks, wl, stream, nrhs=4):
         out[f"fp64_ms_rows{mr}_nrhs{r}"] = round(a.elapsed_time(b), 3)
     out["fp64_note"] = (f"FP64 form, {mr} target rows: {nrhs} right-hand sides in one pass against one; "
                         "w read with stride nrhs in both")
+    return out
+
+
+def run_list_local(args, torch, gsks, k=64, ncl=64, per=2048):
+    """Tree-code-like lists (the batched form's intended use: near-field blocks):
+    64 clusters (centres U[-10,10]^k, sigma 0.05) of 2048 points, one task per
+    cluster (its points against themselves), Gaussian h = 0.2; each task is
+    centred and scaled on its own box.  Wall clock around each synchronous
+    dgsks_list call, device arrays, both forms."""
+    import numpy as np
+    rng = np.random.default_rng(5)
+    centres = rng.uniform(-10, 10, (ncl, k))
+    X = (centres[:, None, :] + 0.05 * rng.standard_normal((ncl, per, k))).reshape(-1, k)
+    N = X.shape[0]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    Xd, wd = dev(X), dev(rng.standard_normal(N))
+    idd = dev(np.arange(N, dtype=np.int32))
+    offd = dev((np.arange(ncl + 1) * per).astype(np.int32))
+    ker = gsks.make_kernel(0, scal=-12.5)
+    pairs = float(ncl) * per * per
+    out = {"workload": f"{ncl} tasks, each one cluster of {per} points against itself (k={k}, mixture centres "
+                       "U[-10,10]^k, sigma 0.05), Gaussian h=0.2", "pairs_per_step": pairs,
+           "timing": "wall clock around each synchronous dgsks_list call, device arrays"}
+    for form in ("split", "fp64"):
+        gsks.set_precision(prec_of(gsks, form))
+        u = torch.zeros(N, dtype=torch.float64, device="cuda")
+        call = lambda: gsks.dgsks_list(ker, u, offd, idd, offd, idd, Xd, None, Xd, None, wd)
+        call()
+        torch.cuda.synchronize()
+        reps = max(1, args.steps) if form == "split" else 1
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            call()
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        out[form] = {"value": pairs / dt, "unit": "pair-evals/s", "ms_per_step": dt * 1e3}
+    gsks.set_precision(gsks.GSKS_FP64)
+    out["split_over_fp64"] = out["split"]["value"] / out["fp64"]["value"]
     return out
 
 
