@@ -38,7 +38,10 @@
 //                resident for the item when k <= 64 (3 source stages), else
 //                both operands streamed in 64-wide k chunks (2 stages)
 //   warp 1       MMA issuer: 6 tcgen05.mma per 16-wide k step into one of two
-//                TMEM accumulator pairs (double buffered, 512 columns)
+//                TMEM accumulator pairs (double buffered, 512 columns); the
+//                whole warp runs the loop, one elected lane issues (the
+//                epilogue warps of its SM sub-partition otherwise starve it
+//                of issue slots and the tensor core idles)
 //   warps 2..17  epilogue: 4 column groups x 4 TMEM sub-partitions, tcgen05.ld
 //                of 16 columns at a time, kernel function, weighted row sums
 // The batched form (KS_LIST) runs the same pipeline over a table of items
@@ -1832,6 +1835,43 @@ __device__ __forceinline__ void epi_chunk_tanh_anchor(const uint32_t (&h)[NC], c
   }
 }
 
+// Row sums of one work item.  The FP32 sums of the 32-column groups
+// accumulate as an unevaluated FP32 pair hi + lo (TwoSum per tile, about
+// 2^-48 relative per addition): FP32 instructions only, since FP64 ones issue
+// at 1/64 of the FP32 rate here and every epilogue warp would queue on that
+// pipe at the end of each tile.  Sums of values rechecked in FP64 enter as
+// their FP32 pair (values below the FP32 range vanish there: a row whose
+// values all lie that low is redone in FP64, and elsewhere they are below
+// 2^-126 against values of the row that are not).
+template <int NR>
+struct RowAcc {
+  float hi[NR], lo[NR];
+  __device__ __forceinline__ void zero()
+  {
+#pragma unroll
+    for (int r = 0; r < NR; r++) { hi[r] = 0.f; lo[r] = 0.f; }
+  }
+  __device__ __forceinline__ void add(int r, float v)
+  {
+    const float s = hi[r] + v;
+    const float bv = s - hi[r];
+    lo[r] += (hi[r] - (s - bv)) + (v - bv);
+    hi[r] = s;
+  }
+  __device__ __forceinline__ void add64(int r, double v)
+  {
+    const float h = (float)v;
+    add(r, h);
+    lo[r] += (float)(v - (double)h);
+  }
+  // the item's row sum r in FP64 (an infinite hi passes through unchanged)
+  __device__ __forceinline__ double total(int r) const
+  {
+    const double h = (double)hi[r];
+    return isfinite(hi[r]) ? h + (double)lo[r] : h;
+  }
+};
+
 // Kernels whose FP32 values may fall below the FP32 range while FP64 keeps
 // them (the row rescue of tile_epilogue).
 __host__ __device__ constexpr bool kt_rescue(int kt)
@@ -1841,7 +1881,7 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 
 // One warp's share of one tile (32 columns of its 32 rows): TMEM loads, kernel
 // values, weighted sums (NR weight columns), rechecks of the flagged pairs.
-// Adds the row sums of these columns to racc[r], and to bsk the columns' sum
+// Adds the row sums of these columns to racc (column r), and to bsk the columns' sum
 // of |w| (over the weight columns) where every value of the 32 columns lies
 // below 2^-96.  The 32 columns are summed in FP32 (four interleaved partial
 // sums) and enter the FP64 row sum with one conversion and one add: FP64
@@ -1849,7 +1889,7 @@ __host__ __device__ constexpr bool kt_rescue(int kt)
 template <int KT, bool LISTED, int NR>
 __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam &T, uint32_t tH, int grp, int row,
                                               const SrcMeta *bm, int ncols, const PtMeta &am, float rc, bool exact,
-                                              bool gfast, const LTab &ltab, double (&racc)[NR],
+                                              bool gfast, const LTab &ltab, RowAcc<NR> &racc,
                                               float &bsk, float *wq)
 {
   // Gaussian kinds with the pools' float-pair copies: flagged pairs are
@@ -1968,8 +2008,8 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   }
 #pragma unroll
   for (int r = 0; r < NR; r++) {
-    racc[r] += (double)fs[r];
-    if (nchk) racc[r] += rchk[r];
+    racc.add(r, fs[r]);
+    if (nchk) racc.add64(r, rchk[r]);
   }
 }
 
@@ -2097,47 +2137,68 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
-    if (lane == 0) {
+    // The whole warp runs the loop (waits and descriptors stay warp-uniform;
+    // a wait's outcome is made uniform with __all_sync), and the elected lane
+    // (lane 0 of the converged warp) issues the MMAs and commits.  A start
+    // address advances the descriptor's address field (address >> 4, 14 bits)
+    // by offset >> 4, without carry for shared-memory addresses below 256 KB.
+    {
+      const unsigned full = 0xffffffffu;
       const uint32_t idesc = idesc_f16_f32(BM, BN);
       const uint32_t lbo = BM * 16, sbo = 128;        // BM == BN
       const uint32_t blk = (uint32_t)BM * L.kc * 2;   // one slice block of one chunk
+      const uint64_t bstep = blk >> 4, sstep = (2 * lbo) >> 4;
+      const int nks = L.kc / 16;
       int g = 0, tc = 0;
       bool stop = false;
-      for (int it = 0; !*abort && !stop; it++) {
-        if (!mbar_wait(&S->a_full, it & 1, abort, a.wait_limit)) break;
-        const int item = ((volatile int *)S->islot)[it & 1];
+      for (int it = 0; !stop; it++) {
+        if (!__all_sync(full, *abort == 0 && mbar_wait(&S->a_full, it & 1, abort, a.wait_limit))) break;
+        const int item = __shfl_sync(full, ((volatile int *)S->islot)[it & 1], 0);
         if (item < 0) break;
         const ItemGeo G = item_geo(a, item);
         for (int tj = G.t0; tj < G.t1 && !stop; tj++, tc++) {
           const int buf = tc & 1;
-          if (tc >= 2 && !mbar_wait(&S->t_empty[buf], ((tc >> 1) - 1) & 1, abort, a.wait_limit)) { stop = true; break; }
+          if (tc >= 2 && !__all_sync(full, mbar_wait(&S->t_empty[buf], ((tc >> 1) - 1) & 1, abort, a.wait_limit))) {
+            stop = true;
+            break;
+          }
           const uint32_t dH = tmem + buf * 256, dL = tmem + buf * 256 + 128;
           for (int c = 0; c < L.nch; c++, g++) {
             const int st = g % L.nstage;
-            if (!mbar_wait(&S->b_full[st], (g / L.nstage) & 1, abort, a.wait_limit)) { stop = true; break; }
+            if (!__all_sync(full, mbar_wait(&S->b_full[st], (g / L.nstage) & 1, abort, a.wait_limit))) {
+              stop = true;
+              break;
+            }
             tc_fence_after();
             const uint32_t sbase = smem_addr(sStage + st * L.stage_bytes);
             const uint32_t a0 = resident ? smem_addr(sA) : sbase;
             const uint32_t b0 = resident ? sbase : sbase + (uint32_t)L.chunk_al;
-            for (int s = 0; s < L.kc / 16; s++) {
-              auto da = [&](int b) { return desc_noswizzle(a0 + b * blk + (uint32_t)s * 2 * lbo, lbo, sbo); };
-              auto db = [&](int b) { return desc_noswizzle(b0 + b * blk + (uint32_t)s * 2 * lbo, lbo, sbo); };
+            const uint64_t dA0 = desc_noswizzle(a0, lbo, sbo), dB0 = desc_noswizzle(b0, lbo, sbo);
+            for (int s = 0; s < nks; s++) {
+              const uint64_t as = dA0 + (uint64_t)s * sstep, bs = dB0 + (uint64_t)s * sstep;
               const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
-              umma_f16(dH, da(0), db(0), idesc, acc);
-              umma_f16(dL, da(0), db(1), idesc, acc);
-              umma_f16(dL, da(1), db(0), idesc, 1);
-              umma_f16(dL, da(1), db(1), idesc, 1);
-              umma_f16(dL, da(0), db(2), idesc, 1);
-              umma_f16(dL, da(2), db(0), idesc, 1);
+              if (elect_one()) {
+                umma_f16(dH, as, bs, idesc, acc);                      // a1 b1
+                umma_f16(dL, as, bs + bstep, idesc, acc);              // a1 b2
+                umma_f16(dL, as + bstep, bs, idesc, 1);                // a2 b1
+                umma_f16(dL, as + bstep, bs + bstep, idesc, 1);        // a2 b2
+                umma_f16(dL, as, bs + 2 * bstep, idesc, 1);            // a1 b3
+                umma_f16(dL, as + 2 * bstep, bs, idesc, 1);            // a3 b1
+              }
+              __syncwarp();
             }
-            umma_commit(&S->b_empty[st]);
+            if (elect_one()) umma_commit(&S->b_empty[st]);
+            __syncwarp();
           }
           if (stop) break;
-          umma_commit(&S->t_full[buf]);
+          if (elect_one()) umma_commit(&S->t_full[buf]);
+          __syncwarp();
         }
-        umma_commit(&S->a_empty);
+        if (elect_one()) umma_commit(&S->a_empty);
+        __syncwarp();
       }
-      umma_commit(&S->drain);
+      if (elect_one()) umma_commit(&S->drain);
+      __syncwarp();
       mbar_wait(&S->drain, 0, &S->never, 1LL << 30);
     }
   } else {
@@ -2172,9 +2233,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       const PtMeta am = ((const PtMeta *)sAmeta)[row];
       __syncwarp();
       if (lane == 0) mbar_arrive(&S->a_empty);
-      double racc[NR];
-#pragma unroll
-      for (int r = 0; r < NR; r++) racc[r] = 0.0;
+      RowAcc<NR> ra;
+      ra.zero();
       float bsk = 0.0f;
       bool ok = true;
       for (int tj = G.t0; tj < G.t1; tj++, g++, tc++) {
@@ -2190,30 +2250,33 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
           const bool lexact = T.exact != 0;
           switch (T.kp.type) {
             case KS_GAUSSIAN:   // scaled units, as a single call
-              tile_epilogue<KS_GAUSSIAN, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_GAUSSIAN, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, T.gfast != 0, ltab, ra, bsk, wq); break;
             case KS_GAUSSIAN_VAR_BANDWIDTH:
-              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_GAUSSIAN_VAR_BANDWIDTH, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, ra, bsk, wq); break;
             case KS_POLYNOMIAL:
-              tile_epilogue<KS_POLYNOMIAL, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_POLYNOMIAL, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, ra, bsk, wq); break;
             case KS_LAPLACE:
-              tile_epilogue<KS_LAPLACE, true, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_LAPLACE, true, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, ra, bsk, wq); break;
             case KS_TANH:
-              tile_epilogue<KS_TANH, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_TANH, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, ra, bsk, wq); break;
             case KS_QUARTIC:
-              tile_epilogue<KS_QUARTIC, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_QUARTIC, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, ra, bsk, wq); break;
             case KS_MULTIQUADRATIC:
-              tile_epilogue<KS_MULTIQUADRATIC, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_MULTIQUADRATIC, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, ra, bsk, wq); break;
             default:
-              tile_epilogue<KS_EPANECHNIKOV, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, racc, bsk, wq); break;
+              tile_epilogue<KS_EPANECHNIKOV, false, 1>(a, T, tH, grp, row, bm, ncols, am, lrc, lexact, false, ltab, ra, bsk, wq); break;
           }
         } else {
-          tile_epilogue<KT, false, NR>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, ltab, racc, bsk, wq);
+          tile_epilogue<KT, false, NR>(a, T, tH, grp, row, bm, ncols, am, rc, exact, gfast, ltab, ra, bsk, wq);
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) { mbar_arrive(&S->t_empty[buf]); mbar_arrive(&S->m_empty[ms]); }
       }
       if (!ok) break;
+      double racc[NR];
+#pragma unroll
+      for (int r = 0; r < NR; r++) racc[r] = ra.total(r);
       if constexpr (NR > 1) {
         // several right-hand sides: every group writes its own partials (no
         // exchange): partial[((r nsc + sc) groups + grp) ldp + i], pskip
