@@ -2173,26 +2173,32 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
             const uint32_t sbase = smem_addr(sStage + st * L.stage_bytes);
             const uint32_t a0 = resident ? smem_addr(sA) : sbase;
             const uint32_t b0 = resident ? sbase : sbase + (uint32_t)L.chunk_al;
+            // every descriptor of the chunk first, then all its MMAs back to
+            // back from the elected lane (no dependent work between them)
             const uint64_t dA0 = desc_noswizzle(a0, lbo, sbo), dB0 = desc_noswizzle(b0, lbo, sbo);
-            for (int s = 0; s < nks; s++) {
-              const uint64_t as = dA0 + (uint64_t)s * sstep, bs = dB0 + (uint64_t)s * sstep;
-              const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
-              if (elect_one()) {
-                umma_f16(dH, as, bs, idesc, acc);                      // a1 b1
-                umma_f16(dL, as, bs + bstep, idesc, acc);              // a1 b2
-                umma_f16(dL, as + bstep, bs, idesc, 1);                // a2 b1
-                umma_f16(dL, as + bstep, bs + bstep, idesc, 1);        // a2 b2
-                umma_f16(dL, as, bs + 2 * bstep, idesc, 1);            // a1 b3
-                umma_f16(dL, as + 2 * bstep, bs, idesc, 1);            // a3 b1
+            uint64_t As[4], Bs[4];
+#pragma unroll
+            for (int s = 0; s < 4; s++) { As[s] = dA0 + (uint64_t)s * sstep; Bs[s] = dB0 + (uint64_t)s * sstep; }
+            const bool last = c == L.nch - 1;
+            if (elect_one()) {
+#pragma unroll
+              for (int s = 0; s < 4; s++) {
+                if (s < nks) {
+                  const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
+                  umma_f16(dH, As[s], Bs[s], idesc, acc);                      // a1 b1
+                  umma_f16(dL, As[s], Bs[s] + bstep, idesc, acc);              // a1 b2
+                  umma_f16(dL, As[s] + bstep, Bs[s], idesc, 1);                // a2 b1
+                  umma_f16(dL, As[s] + bstep, Bs[s] + bstep, idesc, 1);        // a2 b2
+                  umma_f16(dL, As[s], Bs[s] + 2 * bstep, idesc, 1);            // a1 b3
+                  umma_f16(dL, As[s] + 2 * bstep, Bs[s], idesc, 1);            // a3 b1
+                }
               }
-              __syncwarp();
+              umma_commit(&S->b_empty[st]);
+              if (last) umma_commit(&S->t_full[buf]);
             }
-            if (elect_one()) umma_commit(&S->b_empty[st]);
             __syncwarp();
           }
           if (stop) break;
-          if (elect_one()) umma_commit(&S->t_full[buf]);
-          __syncwarp();
         }
         if (elect_one()) umma_commit(&S->a_empty);
         __syncwarp();
