@@ -1044,11 +1044,22 @@ __device__ void laplace_table(float4 *tab, int sh)
   }
 }
 
-// A thread's view of the table: its copy and the copies' stride.
+// A thread's view of the table: its copy and the copies' stride.  An entry is
+// read with one 16-byte shared load (an ordinary float4 read whose last field
+// goes unused is split by the compiler into an 8- and a 4-byte load, which
+// conflict across the copies' banks: twice the shared-memory wavefronts, taken
+// from the tensor core's operand reads).
 struct LTab {
   const float4 *p;      // tab + this lane's copy
   int sh;
-  __device__ __forceinline__ float4 operator[](uint32_t i) const { return p[i << sh]; }
+  __device__ __forceinline__ float4 operator[](uint32_t i) const
+  {
+    float4 v;
+    asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "r"(smem_addr(p) + ((i << sh) << 4)));
+    return v;
+  }
 };
 
 // scal * d2^powe for the double-float d2 = t + lo, powe = -P/2, as
