@@ -1391,6 +1391,37 @@ __device__ __forceinline__ void ff_dist2_warp(const float2 *__restrict__ x, cons
 // pair (ff_dist2_warp), shorter ones by one lane per pair (ff_dist2).
 constexpr int WARP_RECHECK_K = 256;
 
+// One flagged Laplace pair, rechecked by the whole warp: the float-pair
+// distance with the lanes over the coordinates (ff_dist2_warp, whose butterfly
+// leaves the same th + tl in every lane), then the table-driven value, in FP64
+// in every lane.  Coincident and overflowing pairs, values beyond the FP64
+// normal range and pools without the float-pair copies go through recheck64
+// on lane 0.  (One lane per pair would chain a row's dependent loads while the
+// other 31 lanes wait, and every warp of the block waits for that warp at the
+// next accumulator buffer.)
+__device__ double recheck_lap_warp(const TileArgs &a, const TaskParam &T, const LTab &ltab, int ipos, int jpos)
+{
+  int pa = a.amap ? a.amap[ipos] : ipos;
+  int pb = a.bmap ? a.bmap[jpos] : jpos;
+  if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
+  if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
+  if (a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag)) {   // the copies exist
+    const float2 *x = a.XAf + (size_t)(a.ffpos ? ipos : pa) * a.k;
+    const float2 *y = a.XBf + (size_t)(a.ffpos ? jpos : pb) * a.k;
+    float th, tl;
+    ff_dist2_warp(x, y, a.k, th, tl);
+    if (th > T.lap.tover && th >= 1e-15f) {
+      int n;
+      const float v = laplace_core(th, tl, ltab, T.lap, n);
+      if (n >= -1020) return scale2(v, n);
+      if (n <= -1090) return 0.0;
+    }
+  }
+  double r = 0.0;
+  if ((threadIdx.x & 31) == 0) r = recheck64<KS_LAPLACE>(a, T.kp, pa, pb);
+  return __shfl_sync(0xffffffffu, r, 0);
+}
+
 // A flagged pair of the Gaussian kinds, FP64-free: the flag rules select pairs
 // whose value lies in the FP32 range, so the value (float-pair distance from
 // the pools' float-pair copies, then exp2_prod) times the column's FP32 weight
@@ -1946,6 +1977,33 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
         if (ffp) {
           fl32 |= flags << (part * NCH);
           flags = 0;
+        }
+      }
+      if constexpr (KT == KS_LAPLACE) {
+        // rechecks of the flagged pairs of these columns: the warp takes them
+        // one after another (each lane's own in column order, as below)
+        const unsigned full = 0xffffffffu;
+        const int lane = threadIdx.x & 31;
+        for (uint32_t pend = __ballot_sync(full, flags != 0); pend; pend = __ballot_sync(full, flags != 0)) {
+          const int src = __ffs(pend) - 1;
+          const int j = __ffs(__shfl_sync(full, flags, src)) - 1;
+          if (lane == src) flags &= flags - 1;
+          const int c = c0 + j;
+          const int ipos = __shfl_sync(full, am.pos, src);
+          if (c < ncols && ipos >= 0) {
+            const int jpos = bm->pos[c];
+            const double kv = recheck_lap_warp(a, T, ltab, ipos, jpos);
+            if (lane == src) {
+              if (a.nrecheck) atomicAdd(a.nrecheck, 1ull);
+#pragma unroll
+              for (int r = 0; r < NR; r++) {
+                const double v = kv * wcol64(a, jpos, r);
+                rchk[r] += v;
+                fchk += fabsf((float)v);
+              }
+              nchk = true;
+            }
+          }
         }
       }
       // rechecks of the flagged pairs of these columns (one lane each)
