@@ -182,8 +182,17 @@ struct __align__(16) TaskParam {
   int anch;              // polynomial of power 1..4 summed around row anchors (as Params::anch)
   float sg;              // scal * g / 2 (anch)
   float nbmax;           // bound of every point's |x''|^2 at the task's scale (the flag test)
+  double kcoin;          // Laplace: the value at coincident points (the reference's clamp), else 0
+  double pad2;
 };
 static_assert(sizeof(TaskParam) % 16 == 0, "TaskParam is copied by the bulk-copy engine");
+
+// Laplace: the value of a pair whose points coincide (d2 below 1e-15 in FP64
+// takes the reference's clamp, d2 = 1.79e308, as recheck64 does).
+__device__ __forceinline__ double lap_coincident(const KParams &kp)
+{
+  return pow_class(1.79e308, kp) * kp.scal;
+}
 
 // One work item of the list form: a target tile and a range of source tiles of
 // one task; the rows' partial sums go to partial[out + row].
@@ -569,6 +578,8 @@ __global__ void task_params_kernel(int ntask, const KParams *__restrict__ kps, c
     T.t_flag = fmaxf(T.t_flag, (float)(c0 * exp2(-120.0 / mm) * 1.001));
     T.lap = lap_param(kp.scal, kp.powe);
   }
+  T.kcoin = kp.type == KS_LAPLACE ? lap_coincident(kp) : 0.0;
+  T.pad2 = 0.0;
   T.any_flag = (T.t_flag > 0.0f || T.rho > 0.0f) ? 1 : 0;
   out[t] = T;
 }
@@ -1344,6 +1355,8 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
           if (n >= -1020) return scale2(y, n);
           if (n <= -1090) return 0.0;
         }
+        // equal points: recheck64's clamp (see recheck_lap_warp)
+        if (th == 0.0f && tl == 0.0f) return T.kcoin;
       }
     }
   }
@@ -1405,6 +1418,7 @@ __device__ double recheck_lap_warp(const TileArgs &a, const TaskParam &T, const 
   int pb = a.bmap ? a.bmap[jpos] : jpos;
   if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
   if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
+  if (pa == pb && a.XA == a.XB) return T.kcoin;   // the same pool point twice
   if (a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag)) {   // the copies exist
     const float2 *x = a.XAf + (size_t)(a.ffpos ? ipos : pa) * a.k;
     const float2 *y = a.XBf + (size_t)(a.ffpos ? jpos : pb) * a.k;
@@ -1416,6 +1430,10 @@ __device__ double recheck_lap_warp(const TileArgs &a, const TaskParam &T, const 
       if (n >= -1020) return scale2(v, n);
       if (n <= -1090) return 0.0;
     }
+    // equal points: every coordinate difference lies below the float-pair
+    // resolution, so the FP64 distance is below 1e-15 as well and takes
+    // recheck64's clamp
+    if (th == 0.0f && tl == 0.0f) return T.kcoin;
   }
   double r = 0.0;
   if ((threadIdx.x & 31) == 0) r = recheck64<KS_LAPLACE>(a, T.kp, pa, pb);
@@ -2297,6 +2315,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
       T0.s2 = (float)s2; T0.s2l = (float)(s2 - (double)T0.s2);
       T0.lap = P->lap; T0.any_flag = P->any_flag; T0.centred = P->centred;
       T0.anch = P->anch; T0.sg = P->sg;
+      T0.kcoin = KT == KS_LAPLACE ? lap_coincident(a.kp) : 0.0;
     }
     int g = 0, tc = 0;
     for (int it = 0; !*abort; it++) {
@@ -2476,6 +2495,7 @@ __global__ void __launch_bounds__(256) split_rescue(TileArgs a, const int *__res
     T.kp = a.kp; T.t_flag = P->t_flag; T.rho = P->rho;
     T.s2 = (float)s2; T.s2l = (float)(s2 - (double)T.s2);
     T.lap = P->lap; T.any_flag = P->any_flag; T.centred = P->centred;
+    T.kcoin = KT == KS_LAPLACE ? lap_coincident(a.kp) : 0.0;
   }
   const int nr = *rcount, lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
