@@ -2011,8 +2011,8 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
           if (c < ncols && ipos >= 0) {
             const int jpos = bm->pos[c];
             const double kv = recheck_lap_warp(a, T, ltab, ipos, jpos);
-            if (lane == src) {
-              if (a.nrecheck) atomicAdd(a.nrecheck, 1ull);
+            if (lane == src && a.nrecheck) atomicAdd(a.nrecheck, 1ull);
+            if (lane == src && kv != 0.0) {   // (coincident points: often exactly 0)
 #pragma unroll
               for (int r = 0; r < NR; r++) {
                 const double v = kv * wcol64(a, jpos, r);
