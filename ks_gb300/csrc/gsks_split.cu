@@ -1322,6 +1322,9 @@ __device__ double recheck(const TileArgs &a, const TaskParam &T, const LTab &lta
   int pb = a.bmap ? a.bmap[jpos] : jpos;
   if (a.nxa >= 0 && (pa < 0 || pa >= a.nxa)) pa = 0;   // flagged by pack_kernel
   if (a.nxb >= 0 && (pb < 0 || pb >= a.nxb)) pb = 0;
+  if constexpr (KT == KS_LAPLACE) {
+    if (pa == pb && a.XA == a.XB) return T.kcoin;   // the same pool point twice
+  }
   if constexpr (KT == KS_GAUSSIAN || KT == KS_GAUSSIAN_VAR_BANDWIDTH ||
                 KT == KS_LAPLACE) {
     if (a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag)) {   // the copies exist
@@ -1997,10 +2000,13 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
           flags = 0;
         }
       }
-      if constexpr (KT == KS_LAPLACE) {
-        // rechecks of the flagged pairs of these columns: the warp takes them
-        // one after another (each lane's own in column order, as below)
-        const unsigned full = 0xffffffffu;
+      // Laplace rechecks of long rows with few flagged pairs in the warp: the
+      // warp takes them one after another (each lane's own in column order,
+      // as below), its lanes over the coordinates.  Short rows, or many
+      // flagged pairs, one lane per pair (the lanes in parallel).
+      constexpr unsigned full = 0xffffffffu;
+      if (KT == KS_LAPLACE && a.k >= 32 && __any_sync(full, flags != 0) &&
+          __reduce_add_sync(full, (unsigned)__popc(flags)) <= 8) {
         const int lane = threadIdx.x & 31;
         for (uint32_t pend = __ballot_sync(full, flags != 0); pend; pend = __ballot_sync(full, flags != 0)) {
           const int src = __ffs(pend) - 1;
