@@ -750,12 +750,15 @@ def run_e2e(args, torch, gsks, wl, ws, form):
                               h["X2"], h["bmap"], h["w"], h["wmap"])
     dt = max_over_ranks(ws, time.perf_counter() - t0)
     gsks.set_precision(gsks.GSKS_FP64)
-    # bytes the host path copies per call: gathered A and B rows, norms, w, u in; u out
+    # bytes the host path moves per call (copied, or read by the gather kernel):
+    # gathered A and B rows, norms, w, u in; u out
     h2d_norm = 8 * (M_T * K_DIM + N_S * K_DIM + M_T + N_S + N_S + M_T)
     h2d_ip = 8 * (M_T * K_DIM + N_S * K_DIM + N_S + M_T)   # the inner-product kernel sends no norms
     return {"value": len(KERNELS) * M_T * N_S * steps * ws / dt, "unit": "pair-evals/s", "form": form,
             "h2d_bytes_per_step": 2 * h2d_norm + h2d_ip, "d2h_bytes_per_step": 8 * M_T * len(KERNELS),
-            "path": "ks.h dgsks() with host numpy arrays (pinned staging inside the call)"}
+            "path": "ks.h dgsks() with host numpy arrays: " + (
+                "rows gathered by a kernel reading the host arrays (the GPU reads pageable host memory)"
+                if gsks.host_gather_on_device() else "rows gathered on the host into pinned staging, then copied")}
 
 
 def cpu_baseline_and_error(args, torch, gsks, wl, forms, stream):

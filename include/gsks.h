@@ -183,6 +183,16 @@ int gsks_probe_peak(int what, double *ops_per_s);
  * reference. */
 int gsks_split_stats(long long *rechecked_pairs, int *rescued_rows);
 
+/* Host-pointer calls (dgsks, dgsks_status, dgsks_ref, dgsks_rhs) gather the
+ * rows their maps name before the kernels run.  Where the device reads
+ * pageable host memory coherently (cudaDevAttrPageableMemoryAccess, as on
+ * Grace-Blackwell), a kernel gathers them straight from the caller's arrays;
+ * elsewhere, or with the environment variable GSKS_HOST_GATHER=cpu, the host
+ * gathers them into pinned buffers and copies those.  Returns 1 for the
+ * first, 0 for the second, on the calling thread's current device (negative:
+ * no CUDA context). */
+int gsks_host_gather_on_device(void);
+
 /* Test hook of the split-precision form (no counterpart in the reference).
  * Sets, for the calling thread's later split-precision calls (dgsks,
  * dgsks_status, gsks_dgsks_device, dgsks_list, ...), the limit of the

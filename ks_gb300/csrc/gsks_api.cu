@@ -164,8 +164,61 @@ static int host_threads_for(size_t work)
 #endif
 }
 
+// One side of a host-pointer call gathered by the GPU straight from the
+// caller's (pageable) host arrays: row i of dX is X[map[i]], and the row's
+// norm, bandwidth and R values (u or w, nrhs interleaved columns) come along.
+// One warp per row, lanes over the coordinates.  The maps were checked on the
+// host first (no negative entry).
+__global__ void __launch_bounds__(256) gather_rows(int cnt, int k, int R, const int *__restrict__ map,
+                                                   const int *__restrict__ vmap, const double *__restrict__ X,
+                                                   const double *__restrict__ X2, const double *__restrict__ hv,
+                                                   const double *__restrict__ val, double *__restrict__ dX,
+                                                   double *__restrict__ dX2, double *__restrict__ dh,
+                                                   double *__restrict__ dval)
+{
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nw) {
+    const int p = map[i], q = vmap[i];
+    const double *src = X + (size_t)p * k;
+    double *dst = dX + (size_t)i * k;
+    for (int e = lane; e < k; e += 32) dst[e] = src[e];
+    if (lane == 0) {
+      if (X2) dX2[i] = X2[p];
+      if (hv) dh[i] = hv[p];
+    }
+    for (int r = lane; r < R; r += 32) dval[(size_t)i * R + r] = val[(size_t)q * R + r];
+  }
+}
+
+// Whether this device's kernels may read pageable host memory (coherent
+// access through the host page tables, as on Grace-Blackwell): then the host
+// calls gather on the GPU.  GSKS_HOST_GATHER=cpu keeps the gather on the host.
+static bool host_direct(Ctx *c)
+{
+  const char *e = getenv("GSKS_HOST_GATHER");
+  if (e && !strcmp(e, "cpu")) return false;
+  if (c->host_direct < 0) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, c->device) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    c->host_direct = v ? 1 : 0;
+  }
+  return c->host_direct == 1;
+}
+
+extern "C" int gsks_host_gather_on_device(void)
+{
+  Ctx *c = get_ctx();
+  if (!c) return -1;
+  return host_direct(c) ? 1 : 0;
+}
+
 // Gather the rows a host-pointer call names into pinned buffers and copy
-// them to the device.  On return `v` describes packed, identity-mapped data.
+// them to the device (or, where the GPU reads host memory, gather them on the
+// GPU).  On return `v` describes packed, identity-mapped data.
 int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
                const double *u, const int *umap,
                const double *XA, const double *XA2, const int *amap,
@@ -189,6 +242,37 @@ int stage_host(Ctx *c, const ks_t *ker, int m, int n, int k,
     ok = c->hhi.ensure((size_t)m * 8) && c->hhj.ensure((size_t)n * 8) &&
          c->dhi.ensure((size_t)m * 8) && c->dhj.ensure((size_t)n * 8);
   if (!ok) return GSKS_ERR_ALLOC;
+
+  if (host_direct(c)) {
+    // the maps are checked on the host (negative entries), then one gather
+    // kernel per side reads the caller's arrays
+    const int nt = host_threads_for((size_t)std::max(m, n) * 16);
+    int bad = 0;
+#pragma omp parallel for num_threads(nt) reduction(| : bad) schedule(static)
+    for (int i = 0; i < std::max(m, n); i++) {
+      if (i < m && (amap[i] < 0 || umap[i] < 0)) bad = 1;
+      if (i < n && (bmap[i] < 0 || wmap[i] < 0)) bad = 1;
+    }
+    if (bad) return GSKS_ERR_MAP_RANGE;
+    const int R_ = (int)R;
+    const int grid = std::max(1, c->num_sms * 8);
+    gather_rows<<<grid, 256, 0, c->stream>>>(m, k, R_, amap, umap, XA, norms ? XA2 : nullptr, varbw ? ker->hi : nullptr,
+                                               u, (double *)c->dA.p, (double *)c->dA2.p, (double *)c->dhi.p,
+                                               (double *)c->du.p);
+    gather_rows<<<grid, 256, 0, c->stream>>>(n, k, R_, bmap, wmap, XB, norms ? XB2 : nullptr, varbw ? ker->hj : nullptr,
+                                               w, (double *)c->dB.p, (double *)c->dB2.p, (double *)c->dhj.p,
+                                               (double *)c->dw.p);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e, "gather_rows");
+    note_launches(2);
+    v.A = (const double *)c->dA.p; v.B = (const double *)c->dB.p;
+    v.A2 = norms ? (const double *)c->dA2.p : nullptr;
+    v.B2 = norms ? (const double *)c->dB2.p : nullptr;
+    v.hi = varbw ? (const double *)c->dhi.p : nullptr;
+    v.hj = varbw ? (const double *)c->dhj.p : nullptr;
+    v.u = (double *)c->du.p; v.w = (const double *)c->dw.p;
+    return GSKS_OK;
+  }
 
   double *hA = (double *)c->hA.p, *hB = (double *)c->hB.p;
   double *hA2 = (double *)c->hA2.p, *hB2 = (double *)c->hB2.p;

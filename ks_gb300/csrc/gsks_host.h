@@ -44,6 +44,7 @@ struct Ctx {
   DevBuf serr;                 // synchronous calls: [0] device error flags, [1] sgsks map-check flag
   DevBuf stats;                // the last split-precision call: rechecked pairs (u64), rescued rows (int)
   int *cur_err = nullptr;      // the error word kernels write (nullptr: err, the asynchronous calls')
+  int host_direct = -1;        // the GPU reads pageable host memory (the host calls' gather), -1: not asked yet
   PinBuf hA, hA2, hB, hB2, hw, hu, hhi, hhj;
   ~Ctx();
 };

@@ -126,6 +126,13 @@ def split_stats() -> dict:
     return {"rechecked_pairs": int(r.value), "rescued_rows": int(q.value)}
 
 
+def host_gather_on_device() -> bool:
+    """Whether host-pointer calls gather their rows with a kernel reading the
+    caller's arrays (devices that read pageable host memory; not with
+    GSKS_HOST_GATHER=cpu) rather than on the host (gsks.h)."""
+    return load().gsks_host_gather_on_device() == 1
+
+
 def split_test_wait(wait_cycles: int = 0, stall: bool = False) -> None:
     """Test hook: bounded-wait limit (clock cycles, 0 = default) and producer
     stall of this thread's later split-precision calls (gsks.h)."""
