@@ -1059,16 +1059,22 @@ __device__ void laplace_table(float4 *tab, int sh)
 // read with one 16-byte shared load (an ordinary float4 read whose last field
 // goes unused is split by the compiler into an 8- and a 4-byte load, which
 // conflict across the copies' banks: twice the shared-memory wavefronts, taken
-// from the tensor core's operand reads).
+// from the tensor core's operand reads).  The entry of an FP32 value with bits
+// u is number (u >> 15) & 255 (its top 8 mantissa bits); its byte offset, that
+// number << (sh + 4), is formed as (u >> (11 - sh)) & (255 << (sh + 4)).
 struct LTab {
-  const float4 *p;      // tab + this lane's copy
-  int sh;
-  __device__ __forceinline__ float4 operator[](uint32_t i) const
+  uint32_t base;        // shared address of this lane's copy
+  int shr;              // 11 - sh
+  uint32_t mask;        // 255 << (sh + 4)
+  __device__ __forceinline__ LTab(const float4 *p, int sh)
+      : base(smem_addr(p)), shr(11 - sh), mask(255u << (sh + 4)) {}
+  // the entry for the FP32 bits u
+  __device__ __forceinline__ float4 at_bits(uint32_t u) const
   {
     float4 v;
     asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
         : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-        : "r"(smem_addr(p) + ((i << sh) << 4)));
+        : "r"(base + ((u >> shr) & mask)));
     return v;
   }
 };
@@ -1085,7 +1091,7 @@ __device__ __forceinline__ float laplace_core(float t, float lo, const LTab &tab
 {
   const uint32_t u = __float_as_uint(t);
   const int e = (int)(u >> 23) - 127;
-  const float4 tb = tab[(u >> 15) & (LTAB - 1)];
+  const float4 tb = tab.at_bits(u);
   const float f = __uint_as_float((u & 0x007fffffu) | 0x3f800000u);
   const float r = fmaf(f, tb.x, -1.0f);
   const float p = r * fmaf(r, fmaf(r, fmaf(r, -0.36067376f, 0.48089835f), -0.72134752f), 1.44269504f);
@@ -1109,7 +1115,7 @@ __device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const 
 {
   const float t0 = lo2(T), t1 = hi2(T);
   const uint32_t u0 = __float_as_uint(t0), u1 = __float_as_uint(t1);
-  const float4 b0 = tab[(u0 >> 15) & (LTAB - 1)], b1 = tab[(u1 >> 15) & (LTAB - 1)];
+  const float4 b0 = tab.at_bits(u0), b1 = tab.at_bits(u1);
   const uint64_t F = pk2(__uint_as_float((u0 & 0x007fffffu) | 0x3f800000u),
                          __uint_as_float((u1 & 0x007fffffu) | 0x3f800000u));
   const uint64_t R = fma2(F, pk2(b0.x, b1.x), pk2(-1.0f, -1.0f));
