@@ -1043,14 +1043,17 @@ __device__ __forceinline__ const TaskParam &pick_task(const TaskParam &slot, con
 // value below 2^-8.8), and -log2(c_i) as an integer on the 2^-12 grid (bits in
 // .z) plus an FP32 remainder (.y).  Filled once per CTA in FP64.
 // Entry i sits at tab[(i << sh) + g] for each of the 2^sh copies g.
-__device__ void laplace_table(float4 *tab, int sh)
+// With L (a single call's Laplace parameters), .w holds c0 - P z (int bits):
+// the entry's part of the exponent, folded (laplace_val2<true>).
+__device__ void laplace_table(float4 *tab, int sh, const LapParam *L = nullptr)
 {
   for (int i = threadIdx.x; i < LTAB; i += blockDim.x) {
     const double fm = 1.0 + (i + 0.5) / LTAB;
     const double c = rint(4096.0 / fm) / 4096.0;
     const double T = -log2(c);
     const double th = rint(T * 4096.0);
-    const float4 v = make_float4((float)c, (float)(T - th / 4096.0), __int_as_float((int)th), 0.f);
+    const float4 v = make_float4((float)c, (float)(T - th / 4096.0), __int_as_float((int)th),
+                                 L ? __int_as_float(L->c0 - L->P * (int)th) : 0.f);
     for (int g = 0; g < (1 << sh); g++) tab[(i << sh) + g] = v;
   }
 }
@@ -1111,6 +1114,8 @@ __device__ __forceinline__ float laplace_val(float t, float lo, const LTab &tab,
 
 // laplace_val of two columns, the floating-point part in packed FP32 pairs (the
 // series one term shorter: its error stays far below the per-pair budget).
+// FOLD: the table was built with this call's parameters (.w = c0 - P z).
+template <bool FOLD = false>
 __device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const LTab &tab, const LapParam &L)
 {
   const float t0 = lo2(T), t1 = hi2(T);
@@ -1127,8 +1132,8 @@ __device__ __forceinline__ uint64_t laplace_val2(uint64_t T, uint64_t LO, const 
   const uint64_t LLO = fma2(mul2(LO, RT), pk2(1.44269504f, 1.44269504f), add2(pk2(b0.y, b1.y), Q));
   // the exponent in 2^-13 units, ls13 - P (4096 (e - 127) + z), with the
   // constant terms folded into c0 and p4096
-  const int E0 = L.c0 - L.p4096 * (int)(u0 >> 23) - L.P * __float_as_int(b0.z);
-  const int E1 = L.c0 - L.p4096 * (int)(u1 >> 23) - L.P * __float_as_int(b1.z);
+  const int E0 = (FOLD ? __float_as_int(b0.w) : L.c0 - L.P * __float_as_int(b0.z)) - L.p4096 * (int)(u0 >> 23);
+  const int E1 = (FOLD ? __float_as_int(b1.w) : L.c0 - L.P * __float_as_int(b1.z)) - L.p4096 * (int)(u1 >> 23);
   // its fraction (E mod 8192) 2^-13 exactly: the float 2^23 + (E & 8191) times
   // 2^-13 is 1024 + fraction, and the FMA with -1024 rounds nothing
   const uint64_t FR = fma2(pk2(__uint_as_float(0x4B000000u | (uint32_t)(E0 & 8191)),
@@ -1652,7 +1657,7 @@ __device__ __forceinline__ void epi_chunk_gfast(const uint32_t (&h)[NC], const u
 
 // NC columns of one row, distance kernels, NR weight columns.  Returns the
 // flagged columns.
-template <int KT, bool EXACT, bool FLAGS, int NC, int NR>
+template <int KT, bool EXACT, bool FLAGS, int NC, int NR, bool FOLD = false>
 __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uint32_t (&l)[NC],
                                               const SrcMeta *__restrict__ bm, int c0, const PtMeta &am, float rc,
                                               const TaskParam &T, const LTab &ltab,
@@ -1685,8 +1690,8 @@ __device__ __forceinline__ uint32_t epi_chunk(const uint32_t (&h)[NC], const uin
     }
     uint64_t KV2[2] = {0, 0};
     if constexpr (KT == KS_LAPLACE) {
-      KV2[0] = laplace_val2(T2[0], LO2[0], ltab, T.lap);
-      KV2[1] = laplace_val2(T2[1], LO2[1], ltab, T.lap);
+      KV2[0] = laplace_val2<FOLD>(T2[0], LO2[0], ltab, T.lap);
+      KV2[1] = laplace_val2<FOLD>(T2[1], LO2[1], ltab, T.lap);
     } else if constexpr (KT == KS_GAUSSIAN_VAR_BANDWIDTH) {
       // factor h_i h_j (negative) as a float pair, two columns at a time
       const uint64_t AH = pk2(am.h, am.h), AHL = pk2(__int_as_float(am.pad[1]), __int_as_float(am.pad[1]));
@@ -1977,6 +1982,8 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
   // float-pair copies of the pools exist (a single call builds them only when
   // it may flag pairs)
   const bool ffp = a.XAf && a.P->ff_ok && (a.tab || a.P->any_flag);
+  // a single call's Laplace table carries the call's exponent constants
+  constexpr bool FOLD = KT == KS_LAPLACE && !LISTED;
   // columns per TMEM load: 8 for the kernels with the most live state per column (the list
   // form's Laplace too: its kernel holds every epilogue variant; and several weight columns)
   constexpr int NCH = (KT == KS_GAUSSIAN_VAR_BANDWIDTH || (KT == KS_LAPLACE && LISTED) || NR > 1) ? 8 : 16;
@@ -1994,11 +2001,11 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
       uint32_t flags = 0;
       const bool fl = T.any_flag != 0;
       if (exact) {
-        if (fl) flags = epi_chunk<KT, true, true, NCH, NR>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
-        else epi_chunk<KT, true, false, NCH, NR>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        if (fl) flags = epi_chunk<KT, true, true, NCH, NR, FOLD>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        else epi_chunk<KT, true, false, NCH, NR, FOLD>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
       } else {
-        if (fl) flags = epi_chunk<KT, false, true, NCH, NR>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
-        else epi_chunk<KT, false, false, NCH, NR>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        if (fl) flags = epi_chunk<KT, false, true, NCH, NR, FOLD>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
+        else epi_chunk<KT, false, false, NCH, NR, FOLD>(h, l, bm, c0, am, rc, T, ltab, acc, amin);
       }
       if constexpr (GK) {
         if (ffp) {
@@ -2152,7 +2159,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) split_tiles(TileArgs a)
   }
   if (warp == 0) { tmem_alloc(&S->tmem_base, TMEM_COLS); tmem_relinquish(); }
   float4 *tab_base = (float4 *)((uint8_t *)S + ((sizeof(SplitSmem) + 15) & ~(size_t)15));
-  if constexpr (KT == KS_LAPLACE || KT == KS_LIST) laplace_table(tab_base, L.tab_sh);
+  if constexpr (KT == KS_LAPLACE || KT == KS_LIST) laplace_table(tab_base, L.tab_sh, KT == KS_LAPLACE ? &a.P->lap : nullptr);
 
   tc_fence_before();
   __syncthreads();
