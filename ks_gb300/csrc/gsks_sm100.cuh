@@ -192,11 +192,12 @@ __device__ __forceinline__ void umma_commit(uint64_t *bar)
                : "memory");
 }
 
-// One lane of the (converged, full) warp: the lowest.  The MMA issuer runs its
-// loop with the whole warp, so that the loop's values stay warp-uniform, and
-// issues each group of MMAs from the elected lane; under a busy SM
-// sub-partition this keeps the tensor core fed at about twice the rate of a
-// loop run by lane 0 alone.
+// One lane of the converged, full warp (elect.sync over all 32 lanes picks the
+// same lane every time, so the MMAs and the commits that track them come from
+// one thread).  The MMA issuer runs its loop with the whole warp, so that the
+// loop's values stay warp-uniform, and issues each group of MMAs from the
+// elected lane; under a busy SM sub-partition this keeps the tensor core fed
+// at about twice the rate of a loop run by lane 0 alone.
 __device__ __forceinline__ bool elect_one()
 {
   uint32_t el;

@@ -1914,9 +1914,12 @@ __device__ __forceinline__ void epi_chunk_tanh_anchor(const uint32_t (&h)[NC], c
 // 2^-48 relative per addition): FP32 instructions only, since FP64 ones issue
 // at 1/64 of the FP32 rate here and every epilogue warp would queue on that
 // pipe at the end of each tile.  Sums of values rechecked in FP64 enter as
-// their FP32 pair (values below the FP32 range vanish there: a row whose
-// values all lie that low is redone in FP64, and elsewhere they are below
-// 2^-126 against values of the row that are not).
+// their FP32 pair when below 2^120 (values below the FP32 range vanish there:
+// a row whose values all lie that low is redone in FP64, and elsewhere they
+// are below 2^-126 against values of the row that are not); a larger one (a
+// Laplace value of nearly coincident points) sends the row to the FP64 redo
+// instead (tile_epilogue).
+constexpr double ROW_PAIR_MAX = 0x1p120;
 template <int NR>
 struct RowAcc {
   float hi[NR], lo[NR];
@@ -2115,7 +2118,12 @@ __device__ __forceinline__ void tile_epilogue(const TileArgs &a, const TaskParam
 #pragma unroll
   for (int r = 0; r < NR; r++) {
     racc.add(r, fs[r]);
-    if (nchk) racc.add64(r, rchk[r]);
+    if (nchk) {
+      // an infinite skipped-group bound makes the reduction redo the row in
+      // FP64 (split_rescue / list_rescue): the value stays out of the pair
+      if (fabs(rchk[r]) < ROW_PAIR_MAX) racc.add64(r, rchk[r]);
+      else if (am.pos >= 0) bsk = __int_as_float(0x7f800000);
+    }
   }
 }
 
